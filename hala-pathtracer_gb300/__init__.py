@@ -1,0 +1,186 @@
+"""GB300 wavefront path tracer: Python host over the libhalapt C ABI.
+
+`Renderer` mirrors the operator surface of the reference's `HalaRenderer`
+(crate hala-renderer as called from src/bin/hala-pathtracer.rs:128-285):
+new -> set_scene -> set_envmap | set_ground_color/set_sky_color ->
+set_env_intensity -> set_exposure_value -> commit -> render ... ->
+save_images, with the same argument meaning. Errors raise `PTError`
+carrying the C status and the library's last-error text, the way the
+reference propagates `anyhow::Result`.
+
+All compute runs in libhalapt.so (hand-written CUDA for sm_103a). There is
+no CPU fallback: if the library is missing or no GPU is present, the
+constructor raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+from . import scenes  # noqa: F401  (procedural workloads)
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libhalapt.so")
+_lib = None
+
+
+class PTError(RuntimeError):
+    def __init__(self, status, message):
+        self.status = status
+        super().__init__(f"{abi.STATUS_NAMES.get(status, status)}: {message}")
+
+
+def load_library(path=None):
+    """Loads libhalapt.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise PTError(abi.PT_ERR_NOT_READY, f"{p} is missing; run build() first")
+        _lib = abi.bind(C.CDLL(p), abi.RENDERER_SIGNATURES)
+    return _lib
+
+
+def build(force=False):
+    from . import buildlib as _b
+    return _b.build(force=force)
+
+
+def _f4(v):
+    v = list(v) + [1.0] * (4 - len(v))
+    return (C.c_float * 4)(*v[:4])
+
+
+class Renderer:
+    """One progressive renderer (HalaRenderer::new, src/bin/hala-pathtracer.rs:128-138)."""
+
+    def __init__(self, config):
+        self._lib = load_library()
+        self.config = config
+        h = C.c_void_p()
+        st = self._lib.pt_renderer_create(C.byref(config), C.byref(h))
+        if st != abi.PT_OK:
+            raise PTError(st, "pt_renderer_create failed (invalid config or no CUDA device)")
+        self._h = h
+        self.width, self.height = config.width, config.height
+        self._keep = []
+
+    # -- lifecycle ---------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.pt_renderer_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st != abi.PT_OK:
+            msg = self._lib.pt_renderer_last_error(self._h)
+            raise PTError(st, msg.decode() if msg else "")
+
+    # -- operator surface ----------------------------------------------------
+    def set_scene(self, scene):
+        """HalaRenderer::set_scene. `scene` is a scenes.Scene or an abi.SceneDesc."""
+        desc = scene.desc() if hasattr(scene, "desc") else scene
+        self._keep = [scene, desc]
+        self._check(self._lib.pt_renderer_set_scene(self._h, C.byref(desc)))
+
+    def set_envmap(self, rgb, rotation_degrees=0.0):
+        """HalaRenderer::set_envmap with decoded pixels: (H, W, 3) float32, row 0 = zenith."""
+        if rgb is None:
+            self._check(self._lib.pt_renderer_set_envmap(self._h, None, 0, 0, 0.0))
+            return
+        a = np.ascontiguousarray(rgb, np.float32)
+        self._check(self._lib.pt_renderer_set_envmap(self._h, a.ctypes.data_as(C.POINTER(C.c_float)),
+                                                     a.shape[1], a.shape[0], float(rotation_degrees)))
+
+    def set_ground_color(self, rgba):
+        self._check(self._lib.pt_renderer_set_ground_color(self._h, _f4(rgba)))
+
+    def set_sky_color(self, rgba):
+        self._check(self._lib.pt_renderer_set_sky_color(self._h, _f4(rgba)))
+
+    def set_env_intensity(self, v):
+        self._check(self._lib.pt_renderer_set_env_intensity(self._h, float(v)))
+
+    def set_exposure_value(self, v):
+        self._check(self._lib.pt_renderer_set_exposure_value(self._h, float(v)))
+
+    def set_camera_index(self, i):
+        self._check(self._lib.pt_renderer_set_camera_index(self._h, int(i)))
+
+    def commit(self):
+        self._check(self._lib.pt_renderer_commit(self._h))
+
+    def render(self, frames=1):
+        """update + render: `frames` progressive frames of 1 sample per pixel."""
+        self._check(self._lib.pt_renderer_render(self._h, int(frames)))
+
+    def reset(self):
+        self._check(self._lib.pt_renderer_reset(self._h))
+
+    def wait_idle(self):
+        self._check(self._lib.pt_renderer_wait_idle(self._h))
+
+    def save_images(self, prefix):
+        """Writes <prefix>_color/_albedo/_normal.pfm and <prefix>_final.ppm."""
+        self._check(self._lib.pt_renderer_save_images(self._h, str(prefix).encode()))
+
+    # -- read-back -----------------------------------------------------------
+    def image(self, which=abi.IMAGE_ACCUM):
+        if which == abi.IMAGE_FINAL:
+            out = np.empty((self.height, self.width, 4), np.uint8)
+        else:
+            out = np.empty((self.height, self.width, 4), np.float32)
+        self._check(self._lib.pt_renderer_read_image(self._h, which, out.ctypes.data, out.nbytes))
+        return out
+
+    def samples(self):
+        """Per-path radiance (n, 3) and hit-sequence hash (n,) of the last render
+        (needs keep_samples); path k is frame k // (W*H), pixel k % (W*H)."""
+        n = self.stats().paths
+        rad = np.empty((n, 3), np.float32)
+        hsh = np.empty((n,), np.uint32)
+        self._check(self._lib.pt_renderer_read_image(self._h, abi.IMAGE_SAMPLE_RADIANCE, rad.ctypes.data, rad.nbytes))
+        self._check(self._lib.pt_renderer_read_image(self._h, abi.IMAGE_SAMPLE_HASH, hsh.ctypes.data, hsh.nbytes))
+        return rad, hsh
+
+    def stats(self):
+        s = abi.Stats()
+        self._check(self._lib.pt_renderer_get_stats(self._h, C.byref(s)))
+        return s
+
+    def stream(self):
+        p = C.c_void_p()
+        self._check(self._lib.pt_renderer_get_stream(self._h, C.byref(p)))
+        return p.value or 0
+
+    def trace_rays(self, rays, any_hit=False, brute_force=False):
+        """rays (n, 8) float32: origin, tmin, direction, tmax -> hits (n, 4) uint32."""
+        rays = np.ascontiguousarray(rays, np.float32)
+        hits = np.empty((len(rays), 4), np.uint32)
+        self._check(self._lib.pt_renderer_trace_rays(self._h, rays.ctypes.data_as(C.POINTER(C.c_float)),
+                                                     len(rays), int(any_hit), int(brute_force),
+                                                     hits.ctypes.data_as(C.POINTER(C.c_uint32))))
+        return hits
+
+
+def renderer_for(scene, **cfg_over):
+    """Creates, fills and commits a renderer for a procedural scene, in the
+    order of src/bin/hala-pathtracer.rs:128-213."""
+    r = Renderer(scene.config(**cfg_over))
+    r.set_scene(scene)
+    if scene.env_rgb is not None:
+        r.set_envmap(scene.env_rgb, scene.env_rotation_deg)
+    else:
+        r.set_ground_color(scene.ground_color)
+        r.set_sky_color(scene.sky_color)
+    r.set_env_intensity(scene.env_intensity)
+    r.set_exposure_value(scene.exposure_value)
+    r.commit()
+    return r

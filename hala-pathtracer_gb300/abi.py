@@ -1,0 +1,157 @@
+"""ctypes mirror of include/hala_pt.h (the C ABI of the GB300 path tracer).
+
+The struct layouts follow shaders/src/hala-pathtracer/inc/types.glsl of the
+reference (Camera :2-11, Light :14-39, Medium :42-49, Material :52-83,
+Vertex/Primitive :86-110) field by field.
+"""
+import ctypes as C
+
+PT_OK = 0
+PT_ERR_INVALID_ARG = 1
+PT_ERR_OOM = 2
+PT_ERR_CUDA = 3
+PT_ERR_TIMEOUT = 4
+PT_ERR_NOT_READY = 5
+PT_ERR_UNSUPPORTED = 6
+PT_ERR_STATE = 7
+PT_ERR_CANCELLED = 8
+
+STATUS_NAMES = {
+    0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA_ERROR", 4: "TIMEOUT",
+    5: "NOT_READY", 6: "UNSUPPORTED", 7: "BAD_STATE", 8: "CANCELLED",
+}
+
+PT_MAX_CAMERAS = 8
+PT_MAX_LIGHTS = 16
+PT_INVALID_INDEX = 0xFFFFFFFF
+
+LIGHT_POINT, LIGHT_DIRECTIONAL, LIGHT_SPOT, LIGHT_QUAD, LIGHT_SPHERE = 0, 1, 2, 3, 4
+MEDIUM_NONE, MEDIUM_ABSORB, MEDIUM_SCATTER, MEDIUM_EMISSIVE = 0, 1, 2, 3
+MATERIAL_DIFFUSE, MATERIAL_DISNEY = 0, 1
+CAMERA_PERSPECTIVE, CAMERA_ORTHOGRAPHIC = 0, 1
+
+IMAGE_ACCUM, IMAGE_ALBEDO, IMAGE_NORMAL, IMAGE_FINAL = 0, 1, 2, 3
+IMAGE_SAMPLE_RADIANCE, IMAGE_SAMPLE_HASH = 4, 5
+
+FEATURE_MEDIUM, FEATURE_VOL_MIS, FEATURE_TRANSPARENT = 1, 2, 4
+
+HIT_MISS = 0xFFFFFFFF
+HIT_LIGHT_BIT = 0x80000000
+
+F3 = C.c_float * 3
+
+
+class Camera(C.Structure):
+    _fields_ = [("position", F3), ("right", F3), ("up", F3), ("forward", F3),
+                ("yfov", C.c_float), ("focal_distance_or_xmag", C.c_float),
+                ("aperture_or_ymag", C.c_float), ("type", C.c_uint32)]
+
+
+class Light(C.Structure):
+    _fields_ = [("intensity", F3), ("position", F3), ("u", F3), ("v", F3),
+                ("radius", C.c_float), ("area", C.c_float), ("type", C.c_int32)]
+
+
+class Medium(C.Structure):
+    _fields_ = [("color", F3), ("density", C.c_float), ("anisotropy", C.c_float),
+                ("type", C.c_uint32)]
+
+
+class Material(C.Structure):
+    _fields_ = [("medium", Medium), ("base_color", F3), ("opacity", C.c_float),
+                ("emission", F3), ("anisotropic", C.c_float), ("metallic", C.c_float),
+                ("roughness", C.c_float), ("subsurface", C.c_float),
+                ("specular_tint", C.c_float), ("sheen", C.c_float), ("sheen_tint", C.c_float),
+                ("clearcoat", C.c_float), ("clearcoat_roughness", C.c_float),
+                ("clearcoat_tint", F3), ("specular_transmission", C.c_float),
+                ("ior", C.c_float), ("ax", C.c_float), ("ay", C.c_float),
+                ("base_color_map_index", C.c_uint32), ("normal_map_index", C.c_uint32),
+                ("metallic_roughness_map_index", C.c_uint32),
+                ("emission_map_index", C.c_uint32), ("type", C.c_uint32)]
+
+
+class Primitive(C.Structure):
+    _fields_ = [("vertices", C.POINTER(C.c_float)), ("num_vertices", C.c_uint32),
+                ("indices", C.POINTER(C.c_uint32)), ("num_indices", C.c_uint32),
+                ("transform", C.c_float * 16), ("material_index", C.c_uint32)]
+
+
+class Texture(C.Structure):
+    _fields_ = [("rgba", C.POINTER(C.c_float)), ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("primitives", C.POINTER(Primitive)), ("num_primitives", C.c_uint32),
+                ("materials", C.POINTER(Material)), ("num_materials", C.c_uint32),
+                ("lights", C.POINTER(Light)), ("num_lights", C.c_uint32),
+                ("cameras", C.POINTER(Camera)), ("num_cameras", C.c_uint32),
+                ("textures", C.POINTER(Texture)), ("num_textures", C.c_uint32)]
+
+
+class TracerConfig(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("max_depth", C.c_uint32),
+                ("rr_depth", C.c_uint32), ("enable_tonemap", C.c_int32),
+                ("enable_aces", C.c_int32), ("use_simple_aces", C.c_int32),
+                ("seed", C.c_uint32), ("max_samples", C.c_uint64),
+                ("wave_paths", C.c_uint32), ("keep_samples", C.c_uint32)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("frame_index", C.c_uint64), ("paths", C.c_uint64),
+                ("closest_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
+                ("render_ms", C.c_double), ("trace_ms", C.c_double),
+                ("bvh_build_ms", C.c_double), ("bvh_nodes", C.c_uint64),
+                ("triangles", C.c_uint64), ("features", C.c_uint32),
+                ("max_bounces_seen", C.c_uint32)]
+
+
+def make_config(width, height, max_depth=8, rr_depth=0, enable_tonemap=True, enable_aces=True,
+                use_simple_aces=False, seed=0, max_samples=0, wave_paths=0, keep_samples=False):
+    cfg = TracerConfig()
+    cfg.width, cfg.height = int(width), int(height)
+    cfg.max_depth, cfg.rr_depth = int(max_depth), int(rr_depth)
+    cfg.enable_tonemap = 1 if enable_tonemap else 0
+    cfg.enable_aces = 1 if enable_aces else 0
+    cfg.use_simple_aces = 1 if use_simple_aces else 0
+    cfg.seed = int(seed)
+    cfg.max_samples = int(max_samples)
+    cfg.wave_paths = int(wave_paths)
+    cfg.keep_samples = 1 if keep_samples else 0
+    return cfg
+
+
+# The exported symbols of libhalapt.so with their ctypes signatures.
+RENDERER_SIGNATURES = {
+    "pt_renderer_create": (C.c_int, [C.POINTER(TracerConfig), C.POINTER(C.c_void_p)]),
+    "pt_renderer_destroy": (None, [C.c_void_p]),
+    "pt_renderer_last_error": (C.c_char_p, [C.c_void_p]),
+    "pt_renderer_set_scene": (C.c_int, [C.c_void_p, C.POINTER(SceneDesc)]),
+    "pt_renderer_set_envmap": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_uint32,
+                                         C.c_uint32, C.c_float]),
+    "pt_renderer_set_ground_color": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    "pt_renderer_set_sky_color": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    "pt_renderer_set_env_intensity": (C.c_int, [C.c_void_p, C.c_float]),
+    "pt_renderer_set_exposure_value": (C.c_int, [C.c_void_p, C.c_float]),
+    "pt_renderer_set_camera_index": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "pt_renderer_commit": (C.c_int, [C.c_void_p]),
+    "pt_renderer_render": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "pt_renderer_reset": (C.c_int, [C.c_void_p]),
+    "pt_renderer_read_image": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t]),
+    "pt_renderer_save_images": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "pt_renderer_wait_idle": (C.c_int, [C.c_void_p]),
+    "pt_renderer_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
+    "pt_renderer_get_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "pt_renderer_trace_rays": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_uint32,
+                                         C.c_int32, C.c_int32, C.POINTER(C.c_uint32)]),
+    "pt_material_preprocess": (None, [C.POINTER(Material)]),
+    "pt_material_default": (None, [C.POINTER(Material)]),
+    "pt_abi_version": (C.c_uint32, []),
+}
+
+
+def bind(lib, signatures):
+    for name, (res, args) in signatures.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib

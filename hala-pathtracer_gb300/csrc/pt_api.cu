@@ -1,0 +1,732 @@
+// pt_api.cu -- the C ABI (include/hala_pt.h): renderer lifecycle, scene
+// upload, progressive rendering, image read-back.
+//
+// Ownership: the renderer owns every device allocation; host arrays passed
+// in are copied before the call returns. Errors never abort: each call
+// returns a pt_status and leaves a message in pt_renderer_last_error().
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "pt_internal.h"
+
+namespace hpt {
+
+int device_sm_count() {
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 132;
+  }
+  return sms;
+}
+
+template <class T>
+struct Buf {
+  T* p = nullptr;
+  size_t n = 0;
+  Buf() = default;
+  Buf(const Buf&) = delete;
+  Buf& operator=(const Buf&) = delete;
+  ~Buf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t ensure(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    release();
+    if (count == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    else p = nullptr;
+    return e;
+  }
+};
+
+}  // namespace hpt
+
+using namespace hpt;
+
+struct pt_renderer {
+  pt_tracer_config cfg{};
+  cudaStream_t stream = nullptr;
+  std::string err;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  uint32_t* pinned = nullptr;
+
+  // scene
+  std::vector<pt_material> mats;
+  std::vector<pt_light> lights;
+  std::vector<pt_camera> cams;
+  uint32_t camera_index = 0;
+  uint32_t nverts = 0, ntris = 0, nnodes = 0;
+  bool has_scene = false, committed = false;
+  Buf<float> raw_verts;
+  Buf<uint32_t> raw_idx;
+  Buf<PrimUpload> dprims;
+  Buf<float4> vnorm, vtan, wpos, tri_v0, tri_e1, tri_e2, tri_sorted, nodes;
+  Buf<float2> vuv;
+  Buf<uint32_t> tri_vidx, tri_mat;
+  Buf<pt_material> dmats;
+
+  // environment
+  bool env_map = false;
+  uint32_t env_w = 0, env_h = 0;
+  float env_rotation = 0.0f, env_intensity = 1.0f;
+  float ground[4] = {0, 0, 0, 1}, sky[4] = {0, 0, 0, 1};
+  float exposure = 0.0f;
+  double env_total = 1.0;
+  Buf<float4> env;
+  Buf<uint2> alias_rows, alias_cols;
+
+  DevScene view{};
+  uint32_t features = 0;
+
+  // wavefront
+  uint32_t wave_cap = 0;
+  Buf<uint4> s_rng;
+  Buf<float4> s_ray_o, s_ray_d, s_hit, s_thr, s_rad, s_albedo, s_normal, s_med0;
+  Buf<float2> s_med1;
+  Buf<float4> s_sh_o, s_sh_d0, s_sh_d1, s_sh_c0, s_sh_c1, s_sh_T;
+  Buf<uint32_t> s_depth, s_flags;
+  Buf<uint32_t> q_a, q_b, q_logic, q_diff, q_dis, q_shadow, counters;
+  Buf<unsigned long long> rays;
+  PathState P{};
+
+  // images
+  Buf<float4> accum, albedo, normal;
+  Buf<uchar4> final_img;
+  Buf<float4> keep_rad;
+  Buf<uint32_t> keep_hash;
+  uint64_t keep_count = 0;
+  uint64_t frame_index = 0;
+  pt_stats stats{};
+};
+
+namespace {
+
+pt_status fail(pt_renderer* r, pt_status s, const std::string& msg) {
+  if (r) r->err = msg;
+  return s;
+}
+pt_status cuda_fail(pt_renderer* r, cudaError_t e, const char* what) {
+  pt_status s = (e == cudaErrorMemoryAllocation) ? PT_ERR_OOM : PT_ERR_CUDA;
+  return fail(r, s, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define CK(r, call)                                         \
+  do {                                                      \
+    cudaError_t e_ = (call);                                \
+    if (e_ != cudaSuccess) return cuda_fail((r), e_, #call); \
+  } while (0)
+
+// Upper-left 3x3 inverse transpose by cofactors (column-major input), the
+// same float operations as the oracle (this file is built without FMA
+// contraction).
+void normal_matrix(const float* T, float N[9]) {
+  auto M = [&](int r, int c) { return T[c * 4 + r]; };
+  float C00 = M(1, 1) * M(2, 2) - M(1, 2) * M(2, 1);
+  float C01 = -(M(1, 0) * M(2, 2) - M(1, 2) * M(2, 0));
+  float C02 = M(1, 0) * M(2, 1) - M(1, 1) * M(2, 0);
+  float C10 = -(M(0, 1) * M(2, 2) - M(0, 2) * M(2, 1));
+  float C11 = M(0, 0) * M(2, 2) - M(0, 2) * M(2, 0);
+  float C12 = -(M(0, 0) * M(2, 1) - M(0, 1) * M(2, 0));
+  float C20 = M(0, 1) * M(1, 2) - M(0, 2) * M(1, 1);
+  float C21 = -(M(0, 0) * M(1, 2) - M(0, 2) * M(1, 0));
+  float C22 = M(0, 0) * M(1, 1) - M(0, 1) * M(1, 0);
+  float det = M(0, 0) * C00 + M(0, 1) * C01 + M(0, 2) * C02;
+  float C[9] = {C00, C01, C02, C10, C11, C12, C20, C21, C22};
+  for (int i = 0; i < 9; ++i) N[i] = C[i] / det;
+}
+
+void fill_view(pt_renderer* r) {
+  DevScene& S = r->view;
+  S = DevScene{};
+  S.tri = r->tri_sorted.p;
+  S.nodes = r->nodes.p;
+  S.tri_vidx = r->tri_vidx.p;
+  S.tri_mat = r->tri_mat.p;
+  S.vnorm = r->vnorm.p;
+  S.vtan = r->vtan.p;
+  S.vuv = r->vuv.p;
+  S.mats = r->dmats.p;
+  S.num_mats = (uint32_t)r->mats.size();
+  S.num_tris = r->ntris;
+  S.num_lights = (uint32_t)r->lights.size();
+  for (uint32_t i = 0; i < S.num_lights; ++i) {
+    const pt_light& l = r->lights[i];
+    DevLight& d = S.lights[i];
+    std::memcpy(d.intensity, l.intensity, 12);
+    std::memcpy(d.position, l.position, 12);
+    std::memcpy(d.u, l.u, 12);
+    std::memcpy(d.v, l.v, 12);
+    d.radius = l.radius;
+    d.area = l.area;
+    d.type = l.type;
+    d.pad = 0;
+  }
+  const pt_camera& c = r->cams[r->camera_index < r->cams.size() ? r->camera_index : 0];
+  std::memcpy(S.cam.position, c.position, 12);
+  std::memcpy(S.cam.right, c.right, 12);
+  std::memcpy(S.cam.up, c.up, 12);
+  std::memcpy(S.cam.forward, c.forward, 12);
+  S.cam.yfov = c.yfov;
+  S.cam.fd_or_xmag = c.focal_distance_or_xmag;
+  S.cam.ap_or_ymag = c.aperture_or_ymag;
+  S.cam.type = c.type;
+  S.env_map = r->env_map ? 1u : 0u;
+  S.env_rgba = r->env.p;
+  S.alias_rows = r->alias_rows.p;
+  S.alias_cols = r->alias_cols.p;
+  S.env_w = r->env_w;
+  S.env_h = r->env_h;
+  S.env_rotation = r->env_rotation;
+  S.env_intensity = r->env_intensity;
+  S.env_total_sum = (float)(r->env_total * (double)r->env_intensity);
+  std::memcpy(S.ground, r->ground, 12);
+  std::memcpy(S.sky, r->sky, 12);
+  S.width = r->cfg.width;
+  S.height = r->cfg.height;
+  S.max_depth = r->cfg.max_depth;
+  S.rr_depth = r->cfg.rr_depth;
+  S.seed = r->cfg.seed;
+  S.features = r->features;
+}
+
+pt_status ensure_wave(pt_renderer* r, uint32_t cap) {
+  if (r->wave_cap >= cap && r->s_rng.p) return PT_OK;
+  const bool med = (r->features & PT_FEATURE_MEDIUM) != 0;
+  CK(r, r->s_rng.ensure(cap));
+  CK(r, r->s_ray_o.ensure(cap));
+  CK(r, r->s_ray_d.ensure(cap));
+  CK(r, r->s_hit.ensure(cap));
+  CK(r, r->s_thr.ensure(cap));
+  CK(r, r->s_rad.ensure(cap));
+  CK(r, r->s_albedo.ensure(cap));
+  CK(r, r->s_normal.ensure(cap));
+  CK(r, r->s_depth.ensure(cap));
+  CK(r, r->s_flags.ensure(cap));
+  if (med) {
+    CK(r, r->s_med0.ensure(cap));
+    CK(r, r->s_med1.ensure(cap));
+  }
+  CK(r, r->s_sh_o.ensure(cap));
+  CK(r, r->s_sh_d0.ensure(cap));
+  CK(r, r->s_sh_d1.ensure(cap));
+  CK(r, r->s_sh_c0.ensure(cap));
+  CK(r, r->s_sh_c1.ensure(cap));
+  CK(r, r->s_sh_T.ensure(cap));
+  CK(r, r->q_a.ensure(cap));
+  CK(r, r->q_b.ensure(cap));
+  CK(r, r->q_logic.ensure(cap));
+  CK(r, r->q_diff.ensure(cap));
+  CK(r, r->q_dis.ensure(cap));
+  CK(r, r->q_shadow.ensure(cap));
+  CK(r, r->counters.ensure(2 * Q_COUNT));
+  CK(r, r->rays.ensure(2));
+  r->wave_cap = cap;
+  PathState& P = r->P;
+  P.rng = r->s_rng.p;
+  P.ray_o = r->s_ray_o.p;
+  P.ray_d = r->s_ray_d.p;
+  P.hit = r->s_hit.p;
+  P.thr = r->s_thr.p;
+  P.rad = r->s_rad.p;
+  P.depth = r->s_depth.p;
+  P.flags = r->s_flags.p;
+  P.albedo = r->s_albedo.p;
+  P.normal = r->s_normal.p;
+  P.med0 = med ? r->s_med0.p : nullptr;
+  P.med1 = med ? r->s_med1.p : nullptr;
+  P.sh_o = r->s_sh_o.p;
+  P.sh_d0 = r->s_sh_d0.p;
+  P.sh_d1 = r->s_sh_d1.p;
+  P.sh_c0 = r->s_sh_c0.p;
+  P.sh_c1 = r->s_sh_c1.p;
+  P.sh_T = r->s_sh_T.p;
+  return PT_OK;
+}
+
+bool write_pfm(const char* path, const float4* px, uint32_t w, uint32_t h) {
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return false;
+  std::fprintf(f, "PF\n%u %u\n-1.0\n", w, h);
+  std::vector<float> row(3 * (size_t)w);
+  for (uint32_t y = 0; y < h; ++y) {
+    const float4* src = px + (size_t)(h - 1 - y) * w;  // PFM rows run bottom to top
+    for (uint32_t x = 0; x < w; ++x) {
+      row[3 * x] = src[x].x;
+      row[3 * x + 1] = src[x].y;
+      row[3 * x + 2] = src[x].z;
+    }
+    std::fwrite(row.data(), sizeof(float), row.size(), f);
+  }
+  return std::fclose(f) == 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+uint32_t pt_abi_version(void) { return PT_ABI_VERSION; }
+
+void pt_material_default(pt_material* m) {
+  if (!m) return;
+  std::memset(m, 0, sizeof(*m));
+  m->base_color[0] = m->base_color[1] = m->base_color[2] = 1.0f;
+  m->opacity = 1.0f;
+  m->clearcoat_tint[0] = m->clearcoat_tint[1] = m->clearcoat_tint[2] = 1.0f;
+  m->ior = 1.5f;
+  m->medium.anisotropy = 0.0f;
+  m->medium.type = PT_MEDIUM_NONE;
+  m->base_color_map_index = m->normal_map_index = PT_INVALID_INDEX;
+  m->metallic_roughness_map_index = m->emission_map_index = PT_INVALID_INDEX;
+  m->type = PT_MATERIAL_DIFFUSE;
+  pt_material_preprocess(m);
+}
+
+// Disney (inc/bxdf/disney.glsl:420): GGX alphas roughness^2 / aspect and
+// roughness^2 * aspect, aspect = sqrt(1 - 0.9 anisotropic), clamped >= 0.001.
+// Diffuse (inc/bxdf/oren_nayar.glsl:35-46): Oren-Nayar A, B with
+// sigma = roughness * pi / 2.
+void pt_material_preprocess(pt_material* m) {
+  if (!m) return;
+  float r = m->roughness;
+  if (m->type == PT_MATERIAL_DISNEY) {
+    float aspect = std::sqrt(1.0f - 0.9f * m->anisotropic);
+    m->ax = std::fmax(0.001f, (r * r) / aspect);
+    m->ay = std::fmax(0.001f, (r * r) * aspect);
+  } else {
+    float sigma = r * 1.57079637f;
+    float s2 = sigma * sigma;
+    m->ax = 1.0f - s2 / (2.0f * (s2 + 0.33f));
+    m->ay = 0.45f * s2 / (s2 + 0.09f);
+  }
+}
+
+pt_status pt_renderer_create(const pt_tracer_config* cfg, pt_renderer** out) {
+  if (!cfg || !out) return PT_ERR_INVALID_ARG;
+  *out = nullptr;
+  // src/config/window.rs:13-21 and src/config/tracer.rs:43-49
+  if (cfg->width == 0 || cfg->height == 0) return PT_ERR_INVALID_ARG;
+  if (cfg->rr_depth > cfg->max_depth) return PT_ERR_INVALID_ARG;
+  if ((uint64_t)cfg->width * cfg->height > (1ull << 31)) return PT_ERR_UNSUPPORTED;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PT_ERR_CUDA;
+  pt_renderer* r = new pt_renderer();
+  r->cfg = *cfg;
+  if (cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&r->ev0) != cudaSuccess || cudaEventCreate(&r->ev1) != cudaSuccess ||
+      cudaMallocHost(&r->pinned, 64) != cudaSuccess) {
+    pt_renderer_destroy(r);
+    return PT_ERR_CUDA;
+  }
+  size_t WH = (size_t)cfg->width * cfg->height;
+  if (r->accum.ensure(WH) || r->albedo.ensure(WH) || r->normal.ensure(WH) || r->final_img.ensure(WH)) {
+    pt_renderer_destroy(r);
+    return PT_ERR_OOM;
+  }
+  cudaMemsetAsync(r->accum.p, 0, WH * sizeof(float4), r->stream);
+  cudaMemsetAsync(r->albedo.p, 0, WH * sizeof(float4), r->stream);
+  cudaMemsetAsync(r->normal.p, 0, WH * sizeof(float4), r->stream);
+  cudaMemsetAsync(r->final_img.p, 0, WH * sizeof(uchar4), r->stream);
+  *out = r;
+  return PT_OK;
+}
+
+void pt_renderer_destroy(pt_renderer* r) {
+  if (!r) return;
+  if (r->stream) cudaStreamSynchronize(r->stream);
+  if (r->ev0) cudaEventDestroy(r->ev0);
+  if (r->ev1) cudaEventDestroy(r->ev1);
+  if (r->pinned) cudaFreeHost(r->pinned);
+  cudaStream_t s = r->stream;
+  delete r;
+  if (s) cudaStreamDestroy(s);
+}
+
+const char* pt_renderer_last_error(const pt_renderer* r) { return r ? r->err.c_str() : "null renderer"; }
+
+pt_status pt_renderer_set_scene(pt_renderer* r, const pt_scene_desc* s) {
+  if (!r) return PT_ERR_INVALID_ARG;
+  if (!s) return fail(r, PT_ERR_INVALID_ARG, "scene is null");
+  if (s->num_cameras == 0 || !s->cameras) return fail(r, PT_ERR_INVALID_ARG, "scene has no camera");
+  if (s->num_cameras > PT_MAX_CAMERAS) return fail(r, PT_ERR_INVALID_ARG, "more than 8 cameras");
+  if (s->num_lights > PT_MAX_LIGHTS) return fail(r, PT_ERR_INVALID_ARG, "more than 16 lights");
+  if (s->num_primitives && !s->primitives) return fail(r, PT_ERR_INVALID_ARG, "primitives is null");
+  if (s->num_materials && !s->materials) return fail(r, PT_ERR_INVALID_ARG, "materials is null");
+  if (s->num_lights && !s->lights) return fail(r, PT_ERR_INVALID_ARG, "lights is null");
+  std::vector<PrimUpload> prims(s->num_primitives);
+  uint64_t nv = 0, nt = 0;
+  for (uint32_t i = 0; i < s->num_primitives; ++i) {
+    const pt_primitive& p = s->primitives[i];
+    if (p.num_indices % 3 != 0) return fail(r, PT_ERR_INVALID_ARG, "index count is not a multiple of 3");
+    if ((p.num_vertices && !p.vertices) || (p.num_indices && !p.indices))
+      return fail(r, PT_ERR_INVALID_ARG, "primitive arrays are null");
+    for (uint32_t k = 0; k < p.num_indices; ++k)
+      if (p.indices[k] >= p.num_vertices) return fail(r, PT_ERR_INVALID_ARG, "index out of range");
+    PrimUpload& u = prims[i];
+    u.vbase = (uint32_t)nv;
+    u.tbase = (uint32_t)nt;
+    u.nverts = p.num_vertices;
+    u.ntris = p.num_indices / 3;
+    for (int row = 0; row < 3; ++row)
+      for (int col = 0; col < 4; ++col) u.xf[row * 4 + col] = p.transform[col * 4 + row];
+    normal_matrix(p.transform, u.nm);
+    u.material = p.material_index;
+    nv += p.num_vertices;
+    nt += p.num_indices / 3;
+  }
+  if (nt >= (1ull << 26) || nv >= (1ull << 31))
+    return fail(r, PT_ERR_UNSUPPORTED, "scene exceeds 2^26 triangles or 2^31 vertices");
+  r->committed = false;
+  r->has_scene = false;
+  r->nverts = (uint32_t)nv;
+  r->ntris = (uint32_t)nt;
+  r->mats.assign(s->materials, s->materials + s->num_materials);
+  r->lights.assign(s->lights, s->lights + s->num_lights);
+  r->cams.assign(s->cameras, s->cameras + s->num_cameras);
+  cudaStream_t st = r->stream;
+  CK(r, r->raw_verts.ensure(11 * (size_t)std::max<uint64_t>(nv, 1)));
+  CK(r, r->raw_idx.ensure(3 * (size_t)std::max<uint64_t>(nt, 1)));
+  CK(r, r->dprims.ensure(std::max<size_t>(prims.size(), 1)));
+  for (uint32_t i = 0; i < s->num_primitives; ++i) {
+    const pt_primitive& p = s->primitives[i];
+    if (p.num_vertices)
+      CK(r, cudaMemcpyAsync(r->raw_verts.p + 11 * (size_t)prims[i].vbase, p.vertices,
+                            11 * sizeof(float) * (size_t)p.num_vertices, cudaMemcpyHostToDevice, st));
+    if (p.num_indices)
+      CK(r, cudaMemcpyAsync(r->raw_idx.p + 3 * (size_t)prims[i].tbase, p.indices, sizeof(uint32_t) * p.num_indices,
+                            cudaMemcpyHostToDevice, st));
+  }
+  if (!prims.empty())
+    CK(r, cudaMemcpyAsync(r->dprims.p, prims.data(), prims.size() * sizeof(PrimUpload), cudaMemcpyHostToDevice, st));
+  size_t V = std::max<uint64_t>(nv, 1), T = std::max<uint64_t>(nt, 1);
+  CK(r, r->vnorm.ensure(V));
+  CK(r, r->vtan.ensure(V));
+  CK(r, r->vuv.ensure(V));
+  CK(r, r->wpos.ensure(V));
+  CK(r, r->tri_v0.ensure(T));
+  CK(r, r->tri_e1.ensure(T));
+  CK(r, r->tri_e2.ensure(T));
+  CK(r, r->tri_vidx.ensure(3 * T));
+  CK(r, r->tri_mat.ensure(T));
+  CK(r, r->dmats.ensure(std::max<size_t>(r->mats.size(), 1)));
+  if (!r->mats.empty())
+    CK(r, cudaMemcpyAsync(r->dmats.p, r->mats.data(), r->mats.size() * sizeof(pt_material), cudaMemcpyHostToDevice,
+                          st));
+  launch_flatten(r->raw_verts.p, r->raw_idx.p, r->dprims.p, (uint32_t)prims.size(), r->nverts, r->ntris, nullptr,
+                 nullptr, r->vnorm.p, r->vtan.p, r->vuv.p, r->wpos.p, r->tri_v0.p, r->tri_e1.p, r->tri_e2.p,
+                 r->tri_vidx.p, r->tri_mat.p, st);
+  CK(r, cudaGetLastError());
+  CK(r, cudaStreamSynchronize(st));
+  r->has_scene = true;
+  return PT_OK;
+}
+
+pt_status pt_renderer_set_envmap(pt_renderer* r, const float* rgb, uint32_t w, uint32_t h, float rot_deg) {
+  if (!r) return PT_ERR_INVALID_ARG;
+  r->committed = false;
+  if (!rgb || w == 0 || h == 0) {
+    r->env_map = false;
+    return PT_OK;
+  }
+  std::vector<float4> px((size_t)w * h);
+  for (size_t i = 0; i < px.size(); ++i) px[i] = make_float4(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2], 0.0f);
+  CK(r, r->env.ensure(px.size()));
+  CK(r, cudaMemcpyAsync(r->env.p, px.data(), px.size() * sizeof(float4), cudaMemcpyHostToDevice, r->stream));
+  CK(r, cudaStreamSynchronize(r->stream));
+  r->env_map = true;
+  r->env_w = w;
+  r->env_h = h;
+  // hdri_rotation is given in degrees (conf/*.yaml); the shaders use turns.
+  r->env_rotation = rot_deg / 360.0f;
+  return PT_OK;
+}
+
+pt_status pt_renderer_set_ground_color(pt_renderer* r, const float rgba[4]) {
+  if (!r || !rgba) return PT_ERR_INVALID_ARG;
+  std::memcpy(r->ground, rgba, 16);
+  r->view.ground[0] = rgba[0]; r->view.ground[1] = rgba[1]; r->view.ground[2] = rgba[2];
+  return PT_OK;
+}
+pt_status pt_renderer_set_sky_color(pt_renderer* r, const float rgba[4]) {
+  if (!r || !rgba) return PT_ERR_INVALID_ARG;
+  std::memcpy(r->sky, rgba, 16);
+  r->view.sky[0] = rgba[0]; r->view.sky[1] = rgba[1]; r->view.sky[2] = rgba[2];
+  return PT_OK;
+}
+pt_status pt_renderer_set_env_intensity(pt_renderer* r, float v) {
+  if (!r) return PT_ERR_INVALID_ARG;
+  r->env_intensity = v;
+  r->view.env_intensity = v;
+  r->view.env_total_sum = (float)(r->env_total * (double)v);
+  return PT_OK;
+}
+pt_status pt_renderer_set_exposure_value(pt_renderer* r, float v) {
+  if (!r) return PT_ERR_INVALID_ARG;
+  r->exposure = v;
+  return PT_OK;
+}
+pt_status pt_renderer_set_camera_index(pt_renderer* r, uint32_t i) {
+  if (!r) return PT_ERR_INVALID_ARG;
+  if (r->has_scene && i >= r->cams.size()) return fail(r, PT_ERR_INVALID_ARG, "camera index out of range");
+  r->camera_index = i;
+  if (r->committed) fill_view(r);
+  return PT_OK;
+}
+
+pt_status pt_renderer_commit(pt_renderer* r) {
+  if (!r) return PT_ERR_INVALID_ARG;
+  if (!r->has_scene) return fail(r, PT_ERR_STATE, "set_scene must come before commit");
+  // feature permutation, src/bin/hala-pathtracer.rs:101-114
+  uint32_t f = 0;
+  for (const pt_material& m : r->mats) {
+    if (m.medium.type != PT_MEDIUM_NONE) f |= PT_FEATURE_MEDIUM | PT_FEATURE_VOL_MIS;
+    if (m.opacity < 1.0f) f |= PT_FEATURE_TRANSPARENT;
+  }
+  const bool wave_layout_changed = ((f ^ r->features) & PT_FEATURE_MEDIUM) != 0;
+  r->features = f;
+  if (wave_layout_changed) r->wave_cap = 0;
+  cudaStream_t st = r->stream;
+  CK(r, r->nodes.ensure(4 * (size_t)std::max<uint32_t>(2 * r->ntris, 2)));
+  CK(r, r->tri_sorted.ensure(3 * (size_t)std::max<uint32_t>(r->ntris, 1)));
+  CK(r, cudaEventRecord(r->ev0, st));
+  if (r->ntris > 0) {
+    BvhBuffers bb{r->nodes.p, r->tri_sorted.p, 2 * r->ntris};
+    uint32_t nn = 0;
+    int rc = build_bvh(r->tri_v0.p, r->tri_e1.p, r->tri_e2.p, r->ntris, bb, &nn, st);
+    if (rc == 2) return fail(r, PT_ERR_OOM, "BVH build: out of device memory");
+    if (rc != 0) return fail(r, PT_ERR_CUDA, "BVH build failed (code " + std::to_string(rc) + ")");
+    r->nnodes = nn;
+  } else {
+    r->nnodes = 0;
+  }
+  CK(r, cudaEventRecord(r->ev1, st));
+  CK(r, cudaEventSynchronize(r->ev1));
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, r->ev0, r->ev1);
+  r->stats.bvh_build_ms = ms;
+  r->stats.bvh_nodes = r->nnodes;
+  r->stats.triangles = r->ntris;
+  if (r->env_map) {
+    const size_t WH = (size_t)r->env_w * r->env_h;
+    Buf<double> q, sums, tot;
+    Buf<uint32_t> stacks;
+    CK(r, q.ensure(2 * WH));
+    CK(r, sums.ensure(r->env_h));
+    CK(r, tot.ensure(1));
+    CK(r, stacks.ensure(2 * WH));
+    CK(r, r->alias_rows.ensure(r->env_h));
+    CK(r, r->alias_cols.ensure(WH));
+    launch_env_tables(r->env.p, r->env_w, r->env_h, r->alias_rows.p, r->alias_cols.p, q.p, stacks.p, sums.p, tot.p,
+                      st);
+    CK(r, cudaGetLastError());
+    CK(r, cudaMemcpyAsync(&r->env_total, tot.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(r, cudaStreamSynchronize(st));
+  }
+  fill_view(r);
+  r->stats.features = f;
+  r->committed = true;
+  return PT_OK;
+}
+
+pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) {
+  if (!r) return PT_ERR_INVALID_ARG;
+  if (!r->committed) return fail(r, PT_ERR_STATE, "commit must come before render");
+  uint64_t nf = frames;
+  if (r->cfg.max_samples > 0) {
+    if (r->frame_index >= r->cfg.max_samples) nf = 0;
+    else nf = std::min<uint64_t>(nf, r->cfg.max_samples - r->frame_index);
+  }
+  const uint32_t WH = r->cfg.width * r->cfg.height;
+  const uint64_t total = nf * WH;
+  r->stats.paths = 0;
+  r->stats.closest_rays = r->stats.shadow_rays = 0;
+  r->stats.render_ms = 0.0;
+  if (total == 0) return PT_OK;
+  uint64_t want = r->cfg.wave_paths ? r->cfg.wave_paths : (1u << 23);
+  uint32_t cap = (uint32_t)std::min<uint64_t>(want, total);
+  pt_status ps = ensure_wave(r, std::max<uint32_t>(cap, r->wave_cap));
+  if (ps != PT_OK) return ps;
+  cap = std::max(cap, r->wave_cap);
+  cudaStream_t st = r->stream;
+  const uint64_t g_start = r->frame_index * WH;
+  if (r->cfg.keep_samples) {
+    CK(r, r->keep_rad.ensure(total));
+    CK(r, r->keep_hash.ensure(total));
+    r->keep_count = total;
+  }
+  CK(r, cudaMemsetAsync(r->rays.p, 0, 2 * sizeof(unsigned long long), st));
+  CK(r, cudaEventRecord(r->ev0, st));
+  uint32_t* cnt0 = r->counters.p;
+  uint32_t* cnt1 = r->counters.p + Q_COUNT;
+  uint32_t max_bounces = 0;
+  for (uint64_t off = 0; off < total; off += cap) {
+    uint32_t n = (uint32_t)std::min<uint64_t>(cap, total - off);
+    uint64_t g0 = g_start + off;
+    launch_camera(r->view, r->P, g0, n, r->q_a.p, cnt1 + Q_NEXT, st);
+    uint32_t live = n;
+    uint32_t b = 0;
+    const uint32_t bounce_cap = 4u * r->cfg.max_depth + 4096u;
+    for (; b < bounce_cap && live > 0; ++b) {
+      uint32_t* out = (b & 1) ? cnt1 : cnt0;
+      uint32_t* in_cnt = ((b & 1) ? cnt0 : cnt1) + Q_NEXT;
+      uint32_t* qin = (b & 1) ? r->q_b.p : r->q_a.p;
+      uint32_t* qnext = (b & 1) ? r->q_a.p : r->q_b.p;
+      CK(r, cudaMemsetAsync(out, 0, Q_COUNT * sizeof(uint32_t), st));
+      QueueSet Q{qin, in_cnt, qnext, r->q_logic.p, r->q_diff.p, r->q_dis.p, r->q_shadow.p, out, r->rays.p};
+      launch_bounce(r->view, r->P, Q, live, st);
+      CK(r, cudaGetLastError());
+      CK(r, cudaMemcpyAsync(r->pinned, out + Q_NEXT, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+      CK(r, cudaStreamSynchronize(st));
+      live = r->pinned[0];
+    }
+    if (live > 0) return fail(r, PT_ERR_TIMEOUT, "paths still alive after the bounce cap");
+    max_bounces = std::max(max_bounces, b);
+    launch_accumulate(r->P, g0, n, WH, r->accum.p, r->albedo.p, r->normal.p,
+                      r->cfg.keep_samples ? r->keep_rad.p : nullptr, r->cfg.keep_samples ? r->keep_hash.p : nullptr,
+                      g_start, st);
+    CK(r, cudaGetLastError());
+  }
+  launch_finalize(r->accum.p, r->final_img.p, WH, r->exposure, r->cfg.enable_tonemap, r->cfg.enable_aces,
+                  r->cfg.use_simple_aces, st);
+  CK(r, cudaGetLastError());
+  CK(r, cudaEventRecord(r->ev1, st));
+  unsigned long long rays[2] = {0, 0};
+  CK(r, cudaMemcpyAsync(rays, r->rays.p, sizeof(rays), cudaMemcpyDeviceToHost, st));
+  CK(r, cudaStreamSynchronize(st));
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, r->ev0, r->ev1);
+  r->frame_index += nf;
+  r->stats.frame_index = r->frame_index;
+  r->stats.paths = total;
+  r->stats.closest_rays = rays[0];
+  r->stats.shadow_rays = rays[1];
+  r->stats.render_ms = ms;
+  r->stats.max_bounces_seen = max_bounces;
+  return PT_OK;
+}
+
+pt_status pt_renderer_reset(pt_renderer* r) {
+  if (!r) return PT_ERR_INVALID_ARG;
+  size_t WH = (size_t)r->cfg.width * r->cfg.height;
+  CK(r, cudaMemsetAsync(r->accum.p, 0, WH * sizeof(float4), r->stream));
+  CK(r, cudaMemsetAsync(r->albedo.p, 0, WH * sizeof(float4), r->stream));
+  CK(r, cudaMemsetAsync(r->normal.p, 0, WH * sizeof(float4), r->stream));
+  CK(r, cudaMemsetAsync(r->final_img.p, 0, WH * sizeof(uchar4), r->stream));
+  CK(r, cudaStreamSynchronize(r->stream));
+  r->frame_index = 0;
+  r->stats.frame_index = 0;
+  return PT_OK;
+}
+
+pt_status pt_renderer_read_image(pt_renderer* r, pt_image which, void* host, size_t bytes) {
+  if (!r) return PT_ERR_INVALID_ARG;
+  if (!host) return fail(r, PT_ERR_INVALID_ARG, "host pointer is null");
+  const size_t WH = (size_t)r->cfg.width * r->cfg.height;
+  CK(r, cudaStreamSynchronize(r->stream));
+  switch (which) {
+    case PT_IMAGE_ACCUM:
+    case PT_IMAGE_ALBEDO:
+    case PT_IMAGE_NORMAL: {
+      if (bytes != WH * sizeof(float4)) return fail(r, PT_ERR_INVALID_ARG, "image size mismatch");
+      const float4* src = which == PT_IMAGE_ACCUM ? r->accum.p : (which == PT_IMAGE_ALBEDO ? r->albedo.p : r->normal.p);
+      CK(r, cudaMemcpy(host, src, bytes, cudaMemcpyDeviceToHost));
+      return PT_OK;
+    }
+    case PT_IMAGE_FINAL:
+      if (bytes != WH * 4) return fail(r, PT_ERR_INVALID_ARG, "image size mismatch");
+      CK(r, cudaMemcpy(host, r->final_img.p, bytes, cudaMemcpyDeviceToHost));
+      return PT_OK;
+    case PT_IMAGE_SAMPLE_RADIANCE: {
+      if (!r->cfg.keep_samples) return fail(r, PT_ERR_STATE, "keep_samples is off");
+      if (bytes != r->keep_count * 12) return fail(r, PT_ERR_INVALID_ARG, "sample buffer size mismatch");
+      std::vector<float4> tmp(r->keep_count);
+      CK(r, cudaMemcpy(tmp.data(), r->keep_rad.p, tmp.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+      float* o = (float*)host;
+      for (size_t i = 0; i < tmp.size(); ++i) {
+        o[3 * i] = tmp[i].x;
+        o[3 * i + 1] = tmp[i].y;
+        o[3 * i + 2] = tmp[i].z;
+      }
+      return PT_OK;
+    }
+    case PT_IMAGE_SAMPLE_HASH:
+      if (!r->cfg.keep_samples) return fail(r, PT_ERR_STATE, "keep_samples is off");
+      if (bytes != r->keep_count * 4) return fail(r, PT_ERR_INVALID_ARG, "sample buffer size mismatch");
+      CK(r, cudaMemcpy(host, r->keep_hash.p, bytes, cudaMemcpyDeviceToHost));
+      return PT_OK;
+  }
+  return fail(r, PT_ERR_INVALID_ARG, "unknown image");
+}
+
+pt_status pt_renderer_save_images(pt_renderer* r, const char* prefix) {
+  if (!r || !prefix) return PT_ERR_INVALID_ARG;
+  const uint32_t W = r->cfg.width, H = r->cfg.height;
+  const size_t WH = (size_t)W * H;
+  std::vector<float4> img(WH);
+  std::string p(prefix);
+  const pt_image kinds[3] = {PT_IMAGE_ACCUM, PT_IMAGE_ALBEDO, PT_IMAGE_NORMAL};
+  const char* names[3] = {"_color.pfm", "_albedo.pfm", "_normal.pfm"};
+  for (int k = 0; k < 3; ++k) {
+    pt_status s = pt_renderer_read_image(r, kinds[k], img.data(), WH * sizeof(float4));
+    if (s != PT_OK) return s;
+    if (!write_pfm((p + names[k]).c_str(), img.data(), W, H))
+      return fail(r, PT_ERR_INVALID_ARG, "cannot write " + p + names[k]);
+  }
+  std::vector<unsigned char> rgba(WH * 4);
+  pt_status s = pt_renderer_read_image(r, PT_IMAGE_FINAL, rgba.data(), rgba.size());
+  if (s != PT_OK) return s;
+  FILE* f = std::fopen((p + "_final.ppm").c_str(), "wb");
+  if (!f) return fail(r, PT_ERR_INVALID_ARG, "cannot write " + p + "_final.ppm");
+  std::fprintf(f, "P6\n%u %u\n255\n", W, H);
+  for (size_t i = 0; i < WH; ++i) std::fwrite(&rgba[4 * i], 1, 3, f);
+  std::fclose(f);
+  return PT_OK;
+}
+
+pt_status pt_renderer_wait_idle(pt_renderer* r) {
+  if (!r) return PT_ERR_INVALID_ARG;
+  CK(r, cudaStreamSynchronize(r->stream));
+  return PT_OK;
+}
+
+pt_status pt_renderer_get_stats(const pt_renderer* r, pt_stats* out) {
+  if (!r || !out) return PT_ERR_INVALID_ARG;
+  *out = r->stats;
+  return PT_OK;
+}
+
+pt_status pt_renderer_get_stream(const pt_renderer* r, void** stream) {
+  if (!r || !stream) return PT_ERR_INVALID_ARG;
+  *stream = (void*)r->stream;
+  return PT_OK;
+}
+
+pt_status pt_renderer_trace_rays(pt_renderer* r, const float* rays, uint32_t n, int32_t any_hit, int32_t brute,
+                                 uint32_t* hits) {
+  if (!r) return PT_ERR_INVALID_ARG;
+  if (!r->committed) return fail(r, PT_ERR_STATE, "commit must come before trace_rays");
+  if (n == 0) return PT_OK;
+  if (!rays || !hits) return fail(r, PT_ERR_INVALID_ARG, "null ray or hit buffer");
+  Buf<float4> dr;
+  Buf<uint4> dh;
+  CK(r, dr.ensure(2 * (size_t)n));
+  CK(r, dh.ensure(n));
+  CK(r, cudaMemcpyAsync(dr.p, rays, 32 * (size_t)n, cudaMemcpyHostToDevice, r->stream));
+  launch_trace_rays(r->view, dr.p, n, any_hit, brute, dh.p, r->stream);
+  CK(r, cudaGetLastError());
+  CK(r, cudaMemcpyAsync(hits, dh.p, 16 * (size_t)n, cudaMemcpyDeviceToHost, r->stream));
+  CK(r, cudaStreamSynchronize(r->stream));
+  return PT_OK;
+}
+
+}  // extern "C"

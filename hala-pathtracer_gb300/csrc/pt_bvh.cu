@@ -1,0 +1,352 @@
+// pt_bvh.cu -- device BVH build (replaces the RT-core acceleration structure
+// that hala-renderer builds for traceRayEXT).
+//
+// Top-down binned SAH, level-synchronous: every level launches one CTA per
+// open task. A CTA bins its task's triangle centroids into 16 bins per axis
+// (bin boxes kept as order-preserving integers in shared memory), picks the
+// cheapest SAH plane, and stably partitions the task's triangle ids into the
+// other ping-pong buffer with a block-wide scan. Leaves (<= 4 triangles, or
+// when SAH says so) copy their ids into the final order. A layout pass then
+// writes the 64-byte traversal nodes and the triangles in leaf order.
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "pt_internal.h"
+
+namespace hpt {
+
+namespace {
+
+constexpr int NB = 16;
+constexpr int BUILD_THREADS = 256;
+constexpr int SAH_LEAF_MAX = 4;
+
+struct BuildNode {
+  float lo[3];
+  float hi[3];
+  int32_t left, right;
+  uint32_t start, count;
+};
+struct BuildTask {
+  uint32_t node, start, count, pad;
+};
+
+__device__ __forceinline__ int f2o(float f) {
+  int i = __float_as_int(f);
+  return i >= 0 ? i : i ^ 0x7FFFFFFF;
+}
+__device__ __forceinline__ float o2f(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7FFFFFFF); }
+
+__device__ __forceinline__ float box_area(float lx, float ly, float lz, float hx, float hy, float hz) {
+  float ex = hx - lx, ey = hy - ly, ez = hz - lz;
+  if (ex < 0.0f) return 0.0f;
+  return 2.0f * (ex * ey + ey * ez + ez * ex);
+}
+
+// Per-triangle bounds (widened by a few ulp) and centroid.
+__global__ void k_prep(const float4* v0, const float4* e1, const float4* e2, uint32_t n, float4* tlo, float4* thi,
+                       float4* tc, uint32_t* ids) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 a = v0[i], b4 = e1[i], c4 = e2[i];
+  float bx = __fadd_rn(a.x, b4.x), by = __fadd_rn(a.y, b4.y), bz = __fadd_rn(a.z, b4.z);
+  float cx = __fadd_rn(a.x, c4.x), cy = __fadd_rn(a.y, c4.y), cz = __fadd_rn(a.z, c4.z);
+  float lx = fminf(a.x, fminf(bx, cx)), ly = fminf(a.y, fminf(by, cy)), lz = fminf(a.z, fminf(bz, cz));
+  float hx = fmaxf(a.x, fmaxf(bx, cx)), hy = fmaxf(a.y, fmaxf(by, cy)), hz = fmaxf(a.z, fmaxf(bz, cz));
+  tc[i] = make_float4((lx + hx) * 0.5f, (ly + hy) * 0.5f, (lz + hz) * 0.5f, 0.0f);
+  auto lo = [](float x) { return x - (fabsf(x) * 4.8e-7f + 1e-30f); };
+  auto hi = [](float x) { return x + (fabsf(x) * 4.8e-7f + 1e-30f); };
+  tlo[i] = make_float4(lo(lx), lo(ly), lo(lz), 0.0f);
+  thi[i] = make_float4(hi(hx), hi(hy), hi(hz), 0.0f);
+  ids[i] = i;
+}
+
+__device__ __forceinline__ float warp_min(float v) {
+  for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+__global__ void __launch_bounds__(BUILD_THREADS) k_level(const BuildTask* tasks, const uint32_t* ntasks_ptr,
+                                                         const uint32_t* src, uint32_t* dst, uint32_t* final_ids,
+                                                         const float4* tlo, const float4* thi, const float4* tc,
+                                                         BuildNode* nodes, uint32_t* node_counter,
+                                                         BuildTask* next_tasks, uint32_t* next_count) {
+  __shared__ float red[12][BUILD_THREADS / 32];
+  __shared__ float box[12];
+  __shared__ int bcnt[3][NB];
+  __shared__ int bmin[3][NB][3];
+  __shared__ int bmax[3][NB][3];
+  __shared__ float cost_s[3 * (NB - 1)];
+  __shared__ int best_s;
+  __shared__ uint32_t wcount[BUILD_THREADS / 32];
+  if (blockIdx.x >= *ntasks_ptr) return;
+  const BuildTask t = tasks[blockIdx.x];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t end = t.start + t.count;
+
+  // 1. box and centroid box
+  float v[12];
+  for (int k = 0; k < 6; ++k) { v[k] = 1e30f; v[6 + k] = -1e30f; }
+  for (uint32_t i = t.start + tid; i < end; i += BUILD_THREADS) {
+    uint32_t id = src[i];
+    float4 lo = tlo[id], hi = thi[id], c = tc[id];
+    v[0] = fminf(v[0], lo.x); v[1] = fminf(v[1], lo.y); v[2] = fminf(v[2], lo.z);
+    v[3] = fminf(v[3], c.x);  v[4] = fminf(v[4], c.y);  v[5] = fminf(v[5], c.z);
+    v[6] = fmaxf(v[6], hi.x); v[7] = fmaxf(v[7], hi.y); v[8] = fmaxf(v[8], hi.z);
+    v[9] = fmaxf(v[9], c.x);  v[10] = fmaxf(v[10], c.y); v[11] = fmaxf(v[11], c.z);
+  }
+  for (int k = 0; k < 6; ++k) { v[k] = warp_min(v[k]); v[6 + k] = warp_max(v[6 + k]); }
+  if (lane == 0)
+    for (int k = 0; k < 12; ++k) red[k][warp] = v[k];
+  __syncthreads();
+  if (tid < 12) {
+    float r = red[tid][0];
+    for (int w = 1; w < BUILD_THREADS / 32; ++w) r = tid < 6 ? fminf(r, red[tid][w]) : fmaxf(r, red[tid][w]);
+    box[tid] = r;
+  }
+  __syncthreads();
+  // box[0..2] lo, [3..5] centroid lo, [6..8] hi, [9..11] centroid hi
+  if (tid == 0) {
+    BuildNode& nd = nodes[t.node];
+    nd.lo[0] = box[0]; nd.lo[1] = box[1]; nd.lo[2] = box[2];
+    nd.hi[0] = box[6]; nd.hi[1] = box[7]; nd.hi[2] = box[8];
+  }
+  const float clo[3] = {box[3], box[4], box[5]};
+  const float cext[3] = {box[9] - box[3], box[10] - box[4], box[11] - box[5]};
+
+  bool leaf = t.count <= 2;
+  int best = -1;
+  if (!leaf) {
+    // 2. bins
+    for (int k = tid; k < 3 * NB; k += BUILD_THREADS) {
+      int a = k / NB, b = k % NB;
+      bcnt[a][b] = 0;
+      for (int c = 0; c < 3; ++c) { bmin[a][b][c] = f2o(1e30f); bmax[a][b][c] = f2o(-1e30f); }
+    }
+    __syncthreads();
+    for (uint32_t i = t.start + tid; i < end; i += BUILD_THREADS) {
+      uint32_t id = src[i];
+      float4 c = tc[id], lo = tlo[id], hi = thi[id];
+      const float cc[3] = {c.x, c.y, c.z};
+      const int ilo[3] = {f2o(lo.x), f2o(lo.y), f2o(lo.z)};
+      const int ihi[3] = {f2o(hi.x), f2o(hi.y), f2o(hi.z)};
+      for (int a = 0; a < 3; ++a) {
+        if (!(cext[a] > 0.0f)) continue;
+        int b = min(NB - 1, max(0, (int)((cc[a] - clo[a]) * ((float)NB / cext[a]))));
+        atomicAdd(&bcnt[a][b], 1);
+        for (int k = 0; k < 3; ++k) {
+          atomicMin(&bmin[a][b][k], ilo[k]);
+          atomicMax(&bmax[a][b][k], ihi[k]);
+        }
+      }
+    }
+    __syncthreads();
+    // 3. SAH cost of every plane
+    if (tid < 3 * (NB - 1)) {
+      int a = tid / (NB - 1), s = tid % (NB - 1);
+      float cost = 3.0e38f;
+      if (cext[a] > 0.0f) {
+        float l[6] = {1e30f, 1e30f, 1e30f, -1e30f, -1e30f, -1e30f}, r[6] = {1e30f, 1e30f, 1e30f, -1e30f, -1e30f, -1e30f};
+        int nl = 0, nr = 0;
+        for (int b = 0; b < NB; ++b) {
+          float* dstb = b <= s ? l : r;
+          int cnt = bcnt[a][b];
+          if (cnt == 0) continue;
+          if (b <= s) nl += cnt; else nr += cnt;
+          for (int k = 0; k < 3; ++k) {
+            dstb[k] = fminf(dstb[k], o2f(bmin[a][b][k]));
+            dstb[3 + k] = fmaxf(dstb[3 + k], o2f(bmax[a][b][k]));
+          }
+        }
+        if (nl > 0 && nr > 0)
+          cost = box_area(l[0], l[1], l[2], l[3], l[4], l[5]) * nl + box_area(r[0], r[1], r[2], r[3], r[4], r[5]) * nr;
+      }
+      cost_s[tid] = cost;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      int bi = -1;
+      float bc = 3.0e38f;
+      for (int k = 0; k < 3 * (NB - 1); ++k)
+        if (cost_s[k] < bc) { bc = cost_s[k]; bi = k; }
+      float area = box_area(box[0], box[1], box[2], box[6], box[7], box[8]);
+      if (bi < 0) {
+        best_s = (t.count <= (uint32_t)LEAF_MAX) ? -2 : -1;  // -2 leaf, -1 median split
+      } else if (t.count <= (uint32_t)SAH_LEAF_MAX && area * t.count <= bc + 0.5f * area) {
+        best_s = -2;
+      } else {
+        best_s = bi;
+      }
+    }
+    __syncthreads();
+    best = best_s;
+    leaf = best == -2;
+  }
+
+  if (leaf) {
+    for (uint32_t i = t.start + tid; i < end; i += BUILD_THREADS) final_ids[i] = src[i];
+    if (tid == 0) {
+      BuildNode& nd = nodes[t.node];
+      nd.left = -1;
+      nd.right = -1;
+      nd.start = t.start;
+      nd.count = t.count;
+    }
+    return;
+  }
+
+  // 4. stable partition into dst
+  uint32_t nleft;
+  if (best < 0) {
+    nleft = t.count / 2;
+    for (uint32_t i = t.start + tid; i < end; i += BUILD_THREADS) dst[i] = src[i];
+  } else {
+    const int a = best / (NB - 1), s = best % (NB - 1);
+    nleft = 0;
+    for (int b = 0; b <= s; ++b) nleft += (uint32_t)bcnt[a][b];
+    const float scale = (float)NB / cext[a];
+    uint32_t lbase = 0, rbase = 0;
+    for (uint32_t base = t.start; base < end; base += BUILD_THREADS) {
+      uint32_t i = base + tid;
+      bool valid = i < end;
+      uint32_t id = valid ? src[i] : 0u;
+      bool left = false;
+      if (valid) {
+        float4 c = tc[id];
+        float cc = a == 0 ? c.x : (a == 1 ? c.y : c.z);
+        int b = min(NB - 1, max(0, (int)((cc - clo[a]) * scale)));
+        left = b <= s;
+      }
+      unsigned m = __ballot_sync(0xffffffffu, left);
+      unsigned mv = __ballot_sync(0xffffffffu, valid);
+      if (lane == 0) wcount[warp] = __popc(m);
+      __syncthreads();
+      uint32_t wl = 0, total_l = 0;
+      for (int w = 0; w < BUILD_THREADS / 32; ++w) {
+        if (w < warp) wl += wcount[w];
+        total_l += wcount[w];
+      }
+      uint32_t chunk = min((uint32_t)BUILD_THREADS, end - base);
+      uint32_t rank_l = wl + __popc(m & ((1u << lane) - 1u));
+      uint32_t before = (uint32_t)(warp * 32) + __popc(mv & ((1u << lane) - 1u));
+      if (valid) {
+        if (left) dst[t.start + lbase + rank_l] = id;
+        else dst[t.start + nleft + rbase + (before - rank_l)] = id;
+      }
+      lbase += total_l;
+      rbase += chunk - total_l;
+      __syncthreads();
+    }
+  }
+  if (tid == 0) {
+    uint32_t c = atomicAdd(node_counter, 2u);
+    BuildNode& nd = nodes[t.node];
+    nd.left = (int32_t)c;
+    nd.right = (int32_t)(c + 1);
+    nd.start = 0;
+    nd.count = 0;
+    uint32_t q = atomicAdd(next_count, 2u);
+    next_tasks[q] = BuildTask{c, t.start, nleft, 0};
+    next_tasks[q + 1] = BuildTask{c + 1, t.start + nleft, t.count - nleft, 0};
+  }
+}
+
+__global__ void k_layout(const BuildNode* nodes, uint32_t nnodes, float4* trav) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nnodes) return;
+  const BuildNode nd = nodes[i];
+  if (nd.left < 0) {
+    if (i == 0) {  // the whole scene is one leaf: wrap it under an internal root
+      trav[0] = make_float4(nd.lo[0], nd.hi[0], nd.lo[1], nd.hi[1]);
+      trav[1] = make_float4(1e30f, 1e30f, 1e30f, 1e30f);
+      trav[2] = make_float4(nd.lo[2], nd.hi[2], 1e30f, 1e30f);
+      trav[3] = make_float4(__int_as_float(make_leaf_link(nd.start, nd.count)),
+                            __int_as_float(make_leaf_link(0, 0)), 0.0f, 0.0f);
+    }
+    return;
+  }
+  const BuildNode L = nodes[nd.left], R = nodes[nd.right];
+  int32_t l0 = L.left < 0 ? make_leaf_link(L.start, L.count) : nd.left;
+  int32_t l1 = R.left < 0 ? make_leaf_link(R.start, R.count) : nd.right;
+  trav[4 * i] = make_float4(L.lo[0], L.hi[0], L.lo[1], L.hi[1]);
+  trav[4 * i + 1] = make_float4(R.lo[0], R.hi[0], R.lo[1], R.hi[1]);
+  trav[4 * i + 2] = make_float4(L.lo[2], L.hi[2], R.lo[2], R.hi[2]);
+  trav[4 * i + 3] = make_float4(__int_as_float(l0), __int_as_float(l1), 0.0f, 0.0f);
+}
+
+__global__ void k_reorder(const uint32_t* final_ids, uint32_t n, const float4* v0, const float4* e1, const float4* e2,
+                          float4* out) {
+  uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  uint32_t id = final_ids[s];
+  float4 a = v0[id];
+  a.w = __uint_as_float(id);
+  out[3 * s] = a;
+  out[3 * s + 1] = e1[id];
+  out[3 * s + 2] = e2[id];
+}
+
+template <class T>
+struct Tmp {
+  T* p = nullptr;
+  cudaError_t alloc(size_t n) { return cudaMalloc(&p, n * sizeof(T)); }
+  ~Tmp() {
+    if (p) cudaFree(p);
+  }
+};
+
+}  // namespace
+
+int build_bvh(const float4* tri_v0, const float4* tri_e1, const float4* tri_e2, uint32_t n, BvhBuffers& out,
+              uint32_t* num_nodes, cudaStream_t st) {
+  if (n == 0) return 0;
+  Tmp<float4> tlo, thi, tc;
+  Tmp<uint32_t> ids_a, ids_b, final_ids, counters;
+  Tmp<BuildTask> tasks_a, tasks_b;
+  Tmp<BuildNode> nodes;
+  const uint32_t cap = 2 * n;
+  if (tlo.alloc(n) || thi.alloc(n) || tc.alloc(n) || ids_a.alloc(n) || ids_b.alloc(n) || final_ids.alloc(n) ||
+      counters.alloc(4) || tasks_a.alloc(n + 1) || tasks_b.alloc(n + 1) || nodes.alloc(cap))
+    return 2;
+  k_prep<<<(n + 255) / 256, 256, 0, st>>>(tri_v0, tri_e1, tri_e2, n, tlo.p, thi.p, tc.p, ids_a.p);
+  // counters: [0] node counter, [1] task count A, [2] task count B
+  BuildTask root{0, 0, n, 0};
+  uint32_t init[4] = {1, 1, 0, 0};
+  cudaMemcpyAsync(tasks_a.p, &root, sizeof(root), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(counters.p, init, sizeof(init), cudaMemcpyHostToDevice, st);
+  uint32_t ntasks = 1;
+  BuildTask* cur = tasks_a.p;
+  BuildTask* nxt = tasks_b.p;
+  uint32_t* src = ids_a.p;
+  uint32_t* dst = ids_b.p;
+  int cur_slot = 1, nxt_slot = 2;
+  uint32_t host_count = 0;
+  for (int level = 0; level < 200 && ntasks > 0; ++level) {
+    cudaMemsetAsync(counters.p + nxt_slot, 0, sizeof(uint32_t), st);
+    k_level<<<ntasks, BUILD_THREADS, 0, st>>>(cur, counters.p + cur_slot, src, dst, final_ids.p, tlo.p, thi.p, tc.p,
+                                              nodes.p, counters.p, nxt, counters.p + nxt_slot);
+    cudaMemcpyAsync(&host_count, counters.p + nxt_slot, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return 3;
+    ntasks = host_count;
+    std::swap(cur, nxt);
+    std::swap(src, dst);
+    std::swap(cur_slot, nxt_slot);
+  }
+  if (ntasks != 0) return 4;
+  uint32_t nn = 0;
+  cudaMemcpyAsync(&nn, counters.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return 3;
+  if (nn > out.node_capacity) return 5;
+  k_layout<<<(nn + 255) / 256, 256, 0, st>>>(nodes.p, nn, out.nodes);
+  k_reorder<<<(n + 255) / 256, 256, 0, st>>>(final_ids.p, n, tri_v0, tri_e1, tri_e2, out.tri_sorted);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return 3;
+  *num_nodes = nn;
+  return 0;
+}
+
+}  // namespace hpt

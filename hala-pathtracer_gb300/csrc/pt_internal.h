@@ -1,0 +1,66 @@
+// pt_internal.h -- host-side interface between the C ABI and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "pt_types.h"
+
+namespace hpt {
+
+// Queues of one bounce (all device pointers).
+struct QueueSet {
+  const uint32_t* in;        // active paths of this bounce
+  const uint32_t* in_count;  // their number
+  uint32_t* next;            // paths continuing to the next bounce
+  uint32_t* logic;
+  uint32_t* diffuse;
+  uint32_t* disney;
+  uint32_t* shadow;
+  uint32_t* counts;            // [Q_COUNT], zeroed at the start of the bounce
+  unsigned long long* rays;    // [0] closest rays, [1] shadow/transmittance rays
+};
+
+int device_sm_count();
+
+// pt_render.cu
+void launch_camera(const DevScene& S, const PathState& P, uint64_t g0, uint32_t n, uint32_t* q_active,
+                   uint32_t* active_count, cudaStream_t st);
+void launch_bounce(const DevScene& S, const PathState& P, const QueueSet& Q, uint32_t max_items, cudaStream_t st);
+void launch_accumulate(const PathState& P, uint64_t g0, uint32_t n, uint32_t WH, float4* accum, float4* albedo,
+                       float4* normal, float4* keep_rad, uint32_t* keep_hash, uint64_t keep_g0, cudaStream_t st);
+void launch_finalize(const float4* accum, uchar4* final_img, uint32_t WH, float ev, int enable, int aces, int simple,
+                     cudaStream_t st);
+void launch_trace_rays(const DevScene& S, const float4* rays, uint32_t n, int any_hit, int brute, uint4* hits,
+                       cudaStream_t st);
+
+// pt_scene.cu: geometry flattening and environment tables
+struct PrimUpload {
+  uint32_t vbase;       // first global vertex
+  uint32_t tbase;       // first global triangle
+  uint32_t nverts, ntris;
+  float xf[12];         // rows of the 3x4 object-to-world matrix
+  float nm[9];          // inverse-transpose of the upper 3x3 (row-major)
+  uint32_t material;
+};
+// Transforms raw vertices (11 floats each) and triangles into world space.
+void launch_flatten(const float* raw_verts, const uint32_t* raw_idx, const PrimUpload* prims, uint32_t nprims,
+                    uint32_t total_verts, uint32_t total_tris, const uint32_t* vert_prim, const uint32_t* tri_prim,
+                    float4* vnorm, float4* vtan, float2* vuv, float4* wpos, float4* tri_v0, float4* tri_e1,
+                    float4* tri_e2, uint32_t* tri_vidx, uint32_t* tri_mat, cudaStream_t st);
+// FP64 alias tables of the environment map; returns the FP64 luminance sum
+// through *total_out (device pointer to one double).
+void launch_env_tables(const float4* env, uint32_t w, uint32_t h, uint2* rows, uint2* cols, double* scratch_q,
+                       uint32_t* scratch_stack, double* row_sums, double* total_out, cudaStream_t st);
+
+// pt_bvh.cu: device BVH build over world-space triangles.
+struct BvhBuffers {
+  float4* nodes;        // output traversal nodes (4 float4 each)
+  float4* tri_sorted;   // output triangles in leaf order (3 float4 each)
+  uint32_t node_capacity;
+};
+// Returns 0 on success; *num_nodes receives the number of nodes used.
+int build_bvh(const float4* tri_v0, const float4* tri_e1, const float4* tri_e2, uint32_t ntris, BvhBuffers& out,
+              uint32_t* num_nodes, cudaStream_t st);
+
+}  // namespace hpt

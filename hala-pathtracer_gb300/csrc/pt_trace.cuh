@@ -1,0 +1,286 @@
+// pt_trace.cuh -- ray/primitive intersection and BVH traversal (device).
+//
+// Replaces the RT-core traversal behind traceRayEXT
+// (pathtracer.rgen.glsl:56-68, inc/lighting.glsl:119-130 / 205-216) and the
+// procedural light intersection shader (lights.rint.glsl:16-37).
+//
+// Closest hit = lexicographic minimum of (t, global triangle id) over all
+// triangles with tmin <= t <= tmax; an analytic light wins only when it is
+// strictly closer. The triangle test uses explicitly rounded operations so
+// it gives bit-identical t/u/v on the CPU oracle (built without FMA
+// contraction), which makes BVH hits comparable bit for bit with brute force.
+#pragma once
+#include "pt_device.cuh"
+#include "pt_types.h"
+
+namespace hpt {
+
+constexpr uint32_t HIT_MISS = 0xFFFFFFFFu;
+constexpr uint32_t HIT_LIGHT_BIT = 0x80000000u;
+
+__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float3 rcross(float3 a, float3 b) {
+  return make_float3(rsub(rmul(a.y, b.z), rmul(a.z, b.y)), rsub(rmul(a.z, b.x), rmul(a.x, b.z)),
+                     rsub(rmul(a.x, b.y), rmul(a.y, b.x)));
+}
+__device__ __forceinline__ float rdot(float3 a, float3 b) {
+  return radd(radd(rmul(a.x, b.x), rmul(a.y, b.y)), rmul(a.z, b.z));
+}
+
+// Moller-Trumbore on (v0, e1, e2); valid when tmin <= t <= tmax.
+__device__ __forceinline__ bool intersect_tri(float3 o, float3 d, float3 v0, float3 e1, float3 e2, float tmin,
+                                              float tmax, float& t, float& u, float& v) {
+  float3 pvec = rcross(d, e2);
+  float det = rdot(e1, pvec);
+  if (det == 0.0f) return false;
+  float inv = __frcp_rn(det);
+  float3 tvec = make_float3(rsub(o.x, v0.x), rsub(o.y, v0.y), rsub(o.z, v0.z));
+  u = rmul(rdot(tvec, pvec), inv);
+  if (u < 0.0f || u > 1.0f) return false;
+  float3 qvec = rcross(tvec, e1);
+  v = rmul(rdot(d, qvec), inv);
+  if (v < 0.0f || radd(u, v) > 1.0f) return false;
+  t = rmul(rdot(e2, qvec), inv);
+  if (t < tmin || t > tmax) return false;
+  return true;
+}
+
+// ------------------------------------------------------------------ lights
+// common/intersection.glsl:31-72, inc/light/quad.glsl:42-60
+__device__ __forceinline__ float quad_intersect(const DevLight& L, float3 o, float3 d, float3& normal, float& pdf) {
+  float3 lu = f3(L.u), lv = f3(L.v), lp = f3(L.position);
+  normal = normalize(cross(lv, lu));
+  float ct = dot(-d, normal);
+  if (ct < 0.0f) return INF;
+  float pw = dot(normal, lp);
+  float3 u = lu / dot(lu, lu);
+  float3 v = lv / dot(lv, lv);
+  float dt = dot(d, normal);
+  float t = (pw - dot(normal, o)) / dt;
+  float tr = INF;
+  if (t > EPS) {
+    float3 p = o + d * t;
+    float3 vi = p - lp;
+    float a1 = dot(u, vi);
+    if (a1 >= 0.0f && a1 <= 1.0f) {
+      float a2 = dot(v, vi);
+      if (a2 >= 0.0f && a2 <= 1.0f) tr = t;
+    }
+  }
+  if (tr < 0.0f) return INF;
+  pdf = (tr * tr) / (L.area * ct);
+  return tr;
+}
+// common/intersection.glsl:6-26, inc/light/sphere.glsl:50-65
+__device__ __forceinline__ float sphere_light_intersect(const DevLight& L, float3 o, float3 d, float& pdf) {
+  float3 lp = f3(L.position);
+  float dist = length(lp - o);
+  if (dist < L.radius) return INF;
+  float3 op = lp - o;
+  float b = dot(op, d);
+  float det = b * b - dot(op, op) + L.radius * L.radius;
+  float t;
+  if (det < 0.0f) {
+    t = INF;
+  } else {
+    det = sqrtf(det);
+    float t1 = b - det;
+    if (t1 > EPS) t = t1;
+    else {
+      float t2 = b + det;
+      t = (t2 > EPS) ? t2 : INF;
+    }
+  }
+  if (t < 0.0f) return INF;
+  float3 hit = o + t * d;
+  float ct = dot(-d, normalize(hit - lp));
+  pdf = (t * t) / (L.area * ct * 0.5f);
+  return t;
+}
+// lights.rint.glsl:16-37
+__device__ __forceinline__ bool light_hit(const DevLight& L, float3 o, float3 d, float tmin, float tmax, float& t,
+                                          float3& n, float& pdf) {
+  t = INF;
+  n = f3(0.0f);
+  pdf = 1.0f;
+  if (L.type == PT_LIGHT_QUAD) t = quad_intersect(L, o, d, n, pdf);
+  else if (L.type == PT_LIGHT_SPHERE) t = sphere_light_intersect(L, o, d, pdf);
+  else return false;
+  return t >= tmin && t <= tmax;
+}
+
+// ------------------------------------------------------------------ BVH traversal
+struct HitRec {
+  float t, u, v;
+  uint32_t id;
+};
+
+__device__ __forceinline__ void child_slabs(const float4 n0, const float4 n1, const float4 n2, float3 o, float3 inv,
+                                            float tmin, float tmax, bool& h0, bool& h1, float& tn0, float& tn1) {
+  // ray-box slabs for both children; far distance widened by ~2 ulp
+  float ox = o.x * inv.x, oy = o.y * inv.y, oz = o.z * inv.z;
+  float a0 = fmaf(n0.x, inv.x, -ox), b0 = fmaf(n0.y, inv.x, -ox);
+  float a1 = fmaf(n0.z, inv.y, -oy), b1 = fmaf(n0.w, inv.y, -oy);
+  float a2 = fmaf(n2.x, inv.z, -oz), b2 = fmaf(n2.y, inv.z, -oz);
+  float c0 = fmaf(n1.x, inv.x, -ox), d0 = fmaf(n1.y, inv.x, -ox);
+  float c1 = fmaf(n1.z, inv.y, -oy), d1 = fmaf(n1.w, inv.y, -oy);
+  float c2 = fmaf(n2.z, inv.z, -oz), d2 = fmaf(n2.w, inv.z, -oz);
+  tn0 = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), tmin));
+  float tf0 = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), tmax));
+  tn1 = fmaxf(fmaxf(fminf(c0, d0), fminf(c1, d1)), fmaxf(fminf(c2, d2), tmin));
+  float tf1 = fminf(fminf(fmaxf(c0, d0), fmaxf(c1, d1)), fminf(fmaxf(c2, d2), tmax));
+  h0 = tn0 <= tf0 * 1.0000005f;
+  h1 = tn1 <= tf1 * 1.0000005f;
+}
+
+constexpr int TRAV_STACK = 64;
+// Upper bound on node visits of one traversal; a well-formed tree never
+// reaches it, a corrupt one ends the traversal instead of looping.
+constexpr uint32_t TRAV_MAX_VISITS = 1u << 22;
+
+// Closest hit over triangles. Returns id == HIT_MISS when nothing is hit.
+template <bool BRUTE>
+__device__ __forceinline__ HitRec trace_tris_closest(const DevScene& S, float3 o, float3 d, float tmin, float tmax) {
+  HitRec h;
+  h.t = tmax;
+  h.u = h.v = 0.0f;
+  h.id = HIT_MISS;
+  if (BRUTE) {
+    for (uint32_t s = 0; s < S.num_tris; ++s) {
+      float4 a = __ldg(&S.tri[3 * s]), b = __ldg(&S.tri[3 * s + 1]), c = __ldg(&S.tri[3 * s + 2]);
+      uint32_t id = __float_as_uint(a.w);
+      float t, u, v;
+      if (intersect_tri(o, d, f3(a), f3(b), f3(c), tmin, h.t, t, u, v) && (t < h.t || id < h.id)) {
+        h.t = t; h.u = u; h.v = v; h.id = id;
+      }
+    }
+    return h;
+  }
+  if (S.num_tris == 0) return h;
+  float3 inv = make_float3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+  int32_t stack[TRAV_STACK];
+  int sp = 0;
+  int32_t cur = 0;  // root is always internal
+  uint32_t visits = 0;
+  for (;;) {
+    while (cur >= 0) {
+      if (++visits > TRAV_MAX_VISITS) return h;
+      const float4* nd = S.nodes + 4 * cur;
+      float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2);
+      int4 n3 = __ldg(reinterpret_cast<const int4*>(nd + 3));
+      bool h0, h1;
+      float tn0, tn1;
+      child_slabs(n0, n1, n2, o, inv, tmin, h.t, h0, h1, tn0, tn1);
+      if (h0 && h1) {
+        int32_t nearc = n3.x, farc = n3.y;
+        if (tn1 < tn0) { nearc = n3.y; farc = n3.x; }
+        if (sp < TRAV_STACK) stack[sp++] = farc;
+        cur = nearc;
+      } else if (h0) {
+        cur = n3.x;
+      } else if (h1) {
+        cur = n3.y;
+      } else {
+        cur = sp > 0 ? stack[--sp] : 0x7FFFFFFF;
+        if (cur == 0x7FFFFFFF) return h;
+      }
+    }
+    // leaf
+    uint32_t start = (uint32_t)cur & 0x03FFFFFFu, count = ((uint32_t)cur >> 26) & 0x1Fu;
+    for (uint32_t s = start; s < start + count; ++s) {
+      float4 a = __ldg(&S.tri[3 * s]), b = __ldg(&S.tri[3 * s + 1]), c = __ldg(&S.tri[3 * s + 2]);
+      uint32_t id = __float_as_uint(a.w);
+      float t, u, v;
+      if (intersect_tri(o, d, f3(a), f3(b), f3(c), tmin, h.t, t, u, v) && (t < h.t || id < h.id)) {
+        h.t = t; h.u = u; h.v = v; h.id = id;
+      }
+    }
+    if (sp == 0) return h;
+    cur = stack[--sp];
+  }
+}
+
+template <bool BRUTE>
+__device__ __forceinline__ bool trace_tris_any(const DevScene& S, float3 o, float3 d, float tmin, float tmax) {
+  if (BRUTE) {
+    for (uint32_t s = 0; s < S.num_tris; ++s) {
+      float4 a = __ldg(&S.tri[3 * s]), b = __ldg(&S.tri[3 * s + 1]), c = __ldg(&S.tri[3 * s + 2]);
+      float t, u, v;
+      if (intersect_tri(o, d, f3(a), f3(b), f3(c), tmin, tmax, t, u, v)) return true;
+    }
+    return false;
+  }
+  if (S.num_tris == 0) return false;
+  float3 inv = make_float3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+  int32_t stack[TRAV_STACK];
+  int sp = 0;
+  int32_t cur = 0;
+  uint32_t visits = 0;
+  for (;;) {
+    while (cur >= 0) {
+      if (++visits > TRAV_MAX_VISITS) return false;
+      const float4* nd = S.nodes + 4 * cur;
+      float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2);
+      int4 n3 = __ldg(reinterpret_cast<const int4*>(nd + 3));
+      bool h0, h1;
+      float tn0, tn1;
+      child_slabs(n0, n1, n2, o, inv, tmin, tmax, h0, h1, tn0, tn1);
+      if (h0 && h1) {
+        int32_t nearc = n3.x, farc = n3.y;
+        if (tn1 < tn0) { nearc = n3.y; farc = n3.x; }
+        if (sp < TRAV_STACK) stack[sp++] = farc;
+        cur = nearc;
+      } else if (h0) {
+        cur = n3.x;
+      } else if (h1) {
+        cur = n3.y;
+      } else {
+        if (sp == 0) return false;
+        cur = stack[--sp];
+      }
+    }
+    uint32_t start = (uint32_t)cur & 0x03FFFFFFu, count = ((uint32_t)cur >> 26) & 0x1Fu;
+    for (uint32_t s = start; s < start + count; ++s) {
+      float4 a = __ldg(&S.tri[3 * s]), b = __ldg(&S.tri[3 * s + 1]), c = __ldg(&S.tri[3 * s + 2]);
+      float t, u, v;
+      if (intersect_tri(o, d, f3(a), f3(b), f3(c), tmin, tmax, t, u, v)) return true;
+    }
+    if (sp == 0) return false;
+    cur = stack[--sp];
+  }
+}
+
+// Closest hit including the analytic light geometry. For a light hit,
+// u = light pdf (the hit attribute of lights.rint.glsl).
+template <bool BRUTE>
+__device__ __forceinline__ HitRec trace_closest(const DevScene& S, float3 o, float3 d, float tmin, float tmax) {
+  HitRec h = trace_tris_closest<BRUTE>(S, o, d, tmin, tmax);
+  float lbest = (h.id != HIT_MISS) ? h.t : INF;
+  for (uint32_t i = 0; i < S.num_lights; ++i) {
+    float t, pdf;
+    float3 n;
+    if (light_hit(S.lights[i], o, d, tmin, tmax, t, n, pdf) && t < lbest) {
+      lbest = t;
+      h.t = t;
+      h.u = pdf;
+      h.v = 0.0f;
+      h.id = HIT_LIGHT_BIT | i;
+    }
+  }
+  if (h.id == HIT_MISS) h.t = INF;
+  return h;
+}
+
+template <bool BRUTE>
+__device__ __forceinline__ bool trace_any(const DevScene& S, float3 o, float3 d, float tmin, float tmax) {
+  for (uint32_t i = 0; i < S.num_lights; ++i) {
+    float t, pdf;
+    float3 n;
+    if (light_hit(S.lights[i], o, d, tmin, tmax, t, n, pdf)) return true;
+  }
+  return trace_tris_any<BRUTE>(S, o, d, tmin, tmax);
+}
+
+}  // namespace hpt

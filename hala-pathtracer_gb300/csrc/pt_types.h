@@ -1,0 +1,123 @@
+// pt_types.h -- device data layout of the GB300 wavefront path tracer.
+//
+// HBM layout (one renderer):
+//   scene    tri[3*slot]        float4 x3 per triangle in BVH leaf order:
+//                               (v0.xyz, global id bits), e1, e2   -- 48 B
+//            nodes[4*i]         binary BVH node, 64 B: child boxes + links
+//            tri_vidx[3*id]     global vertex indices of triangle id
+//            tri_mat[id]        material index of triangle id
+//            vnorm/vtan[v]      float4 world-space (un-normalised) attributes
+//            vuv[v]             float2
+//            mats[]             pt_material (the std140 Material field set)
+//            env_rgba[]         float4 per environment texel
+//            alias rows/cols    uint2 (prob bits, alias index) per entry
+//   wave     SoA path state sized for `wave_paths` paths (see PathState)
+//   images   accum/albedo/normal float4 per pixel, final uchar4 per pixel
+#pragma once
+#include <cstdint>
+
+#include "../../include/hala_pt.h"
+
+namespace hpt {
+
+struct DevLight {  // inc/types.glsl:14-39, padded to 64 B
+  float intensity[3];
+  float position[3];
+  float u[3];
+  float v[3];
+  float radius;
+  float area;
+  int32_t type;
+  int32_t pad;
+};
+
+struct DevCamera {  // inc/types.glsl:2-11
+  float position[3];
+  float right[3];
+  float up[3];
+  float forward[3];
+  float yfov, fd_or_xmag, ap_or_ymag;
+  uint32_t type;
+};
+
+// Binary BVH node (64 B = 4 x 16 B loads):
+//   n0 = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
+//   n1 = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
+//   n2 = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
+//   n3 = (link0, link1, 0, 0)
+// link >= 0: internal node index; link < 0: leaf, start = link & 0x03FFFFFF
+// (slot in tri[]), count = (link >> 26) & 0x1F. An empty child has an
+// inverted box so it never intersects.
+constexpr int32_t LEAF_BIT = (int32_t)0x80000000u;
+constexpr int LEAF_MAX = 8;
+
+__host__ __device__ inline int32_t make_leaf_link(uint32_t start, uint32_t count) {
+  return (int32_t)(0x80000000u | (count << 26) | start);
+}
+
+struct DevScene {
+  const float4* tri;
+  const float4* nodes;
+  const uint32_t* tri_vidx;
+  const uint32_t* tri_mat;
+  const float4* vnorm;
+  const float4* vtan;
+  const float2* vuv;
+  const pt_material* mats;
+  uint32_t num_mats;
+  uint32_t num_tris;
+  uint32_t num_lights;
+  uint32_t env_map;  // 0 = sky (ENV_TYPE_SKY), 1 = map
+  DevLight lights[PT_MAX_LIGHTS];
+  DevCamera cam;
+  // environment, inc/global.glsl:11-24
+  const float4* env_rgba;
+  const uint2* alias_rows;  // (prob float bits, alias)
+  const uint2* alias_cols;
+  uint32_t env_w, env_h;
+  float env_rotation, env_intensity, env_total_sum;
+  float ground[3], sky[3];
+  // tracer settings, MainUBO inc/global.glsl:11-30
+  uint32_t width, height, max_depth, rr_depth, seed;
+  uint32_t features;
+};
+
+// Structure-of-arrays path state of one wavefront (capacity P paths).
+struct PathState {
+  uint4* rng;        // s0 of the per-path RNG (s1 is only used by the camera)
+  float4* ray_o;     // origin.xyz
+  float4* ray_d;     // direction.xyz
+  float4* hit;       // t, u, v, id bits (light hit: u = light pdf)
+  float4* thr;       // throughput.xyz, state.pdf
+  float4* rad;       // radiance.xyz, hash bits
+  uint32_t* depth;   // state.depth (uint, wraps like the reference)
+  uint32_t* flags;   // state.flags | ANS_BIT | IN_MEDIUM_BIT | DONE_BIT
+  float4* albedo;    // first-hit albedo
+  float4* normal;    // first-hit normal
+  float4* med0;      // medium color.xyz, density
+  float2* med1;      // medium anisotropy, type bits
+  // pending next-event estimation (non-VOL_MIS): shadow rays + contributions
+  float4* sh_o;      // scatter position, mask bits (1 env, 2 light), events
+  float4* sh_d0;     // env ray dir, tmax
+  float4* sh_d1;     // light ray dir, tmax
+  float4* sh_c0;     // env contribution, (unused)
+  float4* sh_c1;     // light contribution, pending hash events
+  float4* sh_T;      // throughput at the NEE vertex
+};
+
+constexpr uint32_t ANS_BIT = 0x100u;        // any_non_specular_bounce
+constexpr uint32_t IN_MEDIUM_BIT = 0x200u;  // is_in_medium
+
+// Queue counters (device memory)
+enum QueueSlot : int {
+  Q_NEXT = 0,     // paths continuing to the next bounce
+  Q_LOGIC = 1,    // miss / emitter / invalid-material hits
+  Q_DIFFUSE = 2,  // surface hits on diffuse materials
+  Q_DISNEY = 3,   // surface hits on Disney materials
+  Q_SHADOW = 4,   // paths with pending shadow rays
+  C_CLOSEST = 5,  // closest-hit rays traced (64-bit pair: 5,6)
+  C_SHADOW = 7,   // shadow/transmittance rays traced (64-bit pair: 7,8)
+  Q_COUNT = 16
+};
+
+}  // namespace hpt

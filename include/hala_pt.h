@@ -1,0 +1,286 @@
+/*
+ * hala_pt.h -- C ABI of the GB300 wavefront path tracer.
+ *
+ * This header is the drop-in boundary for the per-pixel path-tracing
+ * integrator of hala-pathtracer. The reference drives its integrator through
+ * the `HalaRenderer` operator surface (crate hala-renderer, called from
+ * src/bin/hala-pathtracer.rs); every entry point below names the call it
+ * replaces. The GLSL-side data contract (Camera, Light, Medium, Material,
+ * Vertex, Primitive) is mirrored field by field from
+ * shaders/src/hala-pathtracer/inc/types.glsl so that a host which already
+ * fills those buffers can fill these structs unchanged.
+ *
+ * Conventions
+ *   - Plain C types only; no CUDA or torch types cross this boundary.
+ *   - The library owns all device memory behind opaque handles. Host arrays
+ *     passed in are copied before the call returns.
+ *   - Every call returns a pt_status. On failure the per-handle last-error
+ *     string (pt_renderer_last_error) says why. No call aborts the process.
+ *   - One host thread at a time per pt_renderer.
+ */
+#ifndef HALA_PT_H
+#define HALA_PT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PT_ABI_VERSION 1u
+
+/* Limits and constants, shaders/src/hala-pathtracer/inc/constants.glsl:1-6 */
+#define PT_MAX_CAMERAS 8u
+#define PT_MAX_LIGHTS 16u
+#define PT_INVALID_INDEX 0xFFFFFFFFu
+
+/* Light types, constants.glsl:14-18 */
+#define PT_LIGHT_POINT 0
+#define PT_LIGHT_DIRECTIONAL 1
+#define PT_LIGHT_SPOT 2
+#define PT_LIGHT_QUAD 3
+#define PT_LIGHT_SPHERE 4
+
+/* Medium types, constants.glsl:41-44 */
+#define PT_MEDIUM_NONE 0u
+#define PT_MEDIUM_ABSORB 1u
+#define PT_MEDIUM_SCATTER 2u
+#define PT_MEDIUM_EMISSIVE 3u
+
+/* Material types: callable order src/bin/hala-pathtracer.rs:182-185 */
+#define PT_MATERIAL_DIFFUSE 0u
+#define PT_MATERIAL_DISNEY 1u
+
+/* Camera types, inc/types.glsl:10 */
+#define PT_CAMERA_PERSPECTIVE 0u
+#define PT_CAMERA_ORTHOGRAPHIC 1u
+
+typedef enum pt_status {
+  PT_OK = 0,
+  PT_ERR_INVALID_ARG = 1,
+  PT_ERR_OOM = 2,
+  PT_ERR_CUDA = 3,
+  PT_ERR_TIMEOUT = 4,
+  PT_ERR_NOT_READY = 5,
+  PT_ERR_UNSUPPORTED = 6,
+  PT_ERR_STATE = 7,
+  PT_ERR_CANCELLED = 8
+} pt_status;
+
+/* Camera, inc/types.glsl:2-11. `type` 0 = perspective, 1 = orthographic. */
+typedef struct pt_camera {
+  float position[3];
+  float right[3];
+  float up[3];
+  float forward[3];
+  float yfov;                    /* radians */
+  float focal_distance_or_xmag;  /* focal distance (perspective) / xmag (orthographic) */
+  float aperture_or_ymag;        /* aperture (perspective) / ymag (orthographic) */
+  uint32_t type;
+} pt_camera;
+
+/* Light, inc/types.glsl:14-39. Field meaning per light type is the same. */
+typedef struct pt_light {
+  float intensity[3];
+  float position[3];
+  float u[3];
+  float v[3];
+  float radius;
+  float area;
+  int32_t type;
+} pt_light;
+
+/* Medium, inc/types.glsl:42-49 */
+typedef struct pt_medium {
+  float color[3];
+  float density;
+  float anisotropy;
+  uint32_t type;
+} pt_medium;
+
+/* Material, inc/types.glsl:52-83. `ax`/`ay` are the preprocessed values the
+ * shaders read: GGX alphas for Disney, Oren-Nayar A/B for diffuse. Use
+ * pt_material_preprocess() to derive them from roughness/anisotropic. */
+typedef struct pt_material {
+  pt_medium medium;
+  float base_color[3];
+  float opacity;
+  float emission[3];
+  float anisotropic;
+  float metallic;
+  float roughness;
+  float subsurface;
+  float specular_tint;
+  float sheen;
+  float sheen_tint;
+  float clearcoat;
+  float clearcoat_roughness;
+  float clearcoat_tint[3];
+  float specular_transmission;
+  float ior;
+  float ax;
+  float ay;
+  uint32_t base_color_map_index;
+  uint32_t normal_map_index;
+  uint32_t metallic_roughness_map_index;
+  uint32_t emission_map_index;
+  uint32_t type;
+} pt_material;
+
+/* One mesh primitive, inc/types.glsl:86-110 (Vertex + Primitive).
+ * `vertices` holds 11 floats per vertex in the Vertex order:
+ * position xyz, normal xyz, tangent xyz, tex_coord xy.
+ * `transform` is a column-major 4x4 object-to-world matrix (GLSL mat4). */
+typedef struct pt_primitive {
+  const float* vertices;
+  uint32_t num_vertices;
+  const uint32_t* indices;
+  uint32_t num_indices;
+  float transform[16];
+  uint32_t material_index;
+} pt_primitive;
+
+/* RGBA32F texture for the material maps (bindless set 2, inc/global.glsl:48). */
+typedef struct pt_texture {
+  const float* rgba;
+  uint32_t width;
+  uint32_t height;
+} pt_texture;
+
+/* The CPU scene handed to set_scene (HalaScene in the reference). */
+typedef struct pt_scene_desc {
+  const pt_primitive* primitives;
+  uint32_t num_primitives;
+  const pt_material* materials;
+  uint32_t num_materials;
+  const pt_light* lights;
+  uint32_t num_lights;
+  const pt_camera* cameras;
+  uint32_t num_cameras;
+  const pt_texture* textures;
+  uint32_t num_textures;
+} pt_scene_desc;
+
+/* Tracer configuration: the arguments of HalaRenderer::new,
+ * src/bin/hala-pathtracer.rs:128-138, plus the output size (window size in
+ * the reference, src/config/window.rs:5-9) and an RNG seed offset.
+ * `seed` is added to the frame index when the per-pixel RNG is seeded
+ * (common/wltcRS.glsl:9-19); 0 reproduces the reference exactly. */
+typedef struct pt_tracer_config {
+  uint32_t width;
+  uint32_t height;
+  uint32_t max_depth;
+  uint32_t rr_depth;
+  int32_t enable_tonemap;
+  int32_t enable_aces;
+  int32_t use_simple_aces;
+  uint32_t seed;
+  uint64_t max_samples;   /* 0 = unlimited */
+  uint32_t wave_paths;    /* paths in flight per wavefront; 0 = library default */
+  uint32_t keep_samples;  /* 1 = keep per-path radiance and hit-sequence hash of the last render call */
+} pt_tracer_config;
+
+typedef enum pt_image {
+  PT_IMAGE_ACCUM = 0,        /* RGBA32F running mean of radiance (g_accum_image) */
+  PT_IMAGE_ALBEDO = 1,       /* RGBA32F running mean of first-hit albedo (g_albedo_image) */
+  PT_IMAGE_NORMAL = 2,       /* RGBA32F running mean of first-hit normal (g_normal_image) */
+  PT_IMAGE_FINAL = 3,        /* RGBA8 exposure + tonemap + sRGB (g_final_image) */
+  PT_IMAGE_SAMPLE_RADIANCE = 4, /* float3 per path of the last render call (keep_samples) */
+  PT_IMAGE_SAMPLE_HASH = 5      /* uint32 hit-sequence hash per path (keep_samples) */
+} pt_image;
+
+typedef struct pt_stats {
+  uint64_t frame_index;      /* frames accumulated so far */
+  uint64_t paths;            /* paths traced by the last render call */
+  uint64_t closest_rays;     /* closest-hit rays traced by the last render call */
+  uint64_t shadow_rays;      /* shadow / transmittance rays traced by the last render call */
+  double render_ms;          /* device time of the last render call (CUDA events) */
+  double trace_ms;           /* device time spent in the closest-hit kernel, last call */
+  double bvh_build_ms;       /* device time of the last BVH build */
+  uint64_t bvh_nodes;
+  uint64_t triangles;
+  uint32_t features;         /* PT_FEATURE_* chosen at commit */
+  uint32_t max_bounces_seen;
+} pt_stats;
+
+#define PT_FEATURE_MEDIUM 1u
+#define PT_FEATURE_VOL_MIS 2u
+#define PT_FEATURE_TRANSPARENT 4u
+
+typedef struct pt_renderer pt_renderer;
+
+/* ---- renderer lifecycle: HalaRenderer operator surface -------------------- */
+
+/* HalaRenderer::new (src/bin/hala-pathtracer.rs:128-138). */
+pt_status pt_renderer_create(const pt_tracer_config* config, pt_renderer** out);
+/* Drop of HalaRenderer after wait_idle (src/bin/hala-pathtracer.rs:226-230). */
+void pt_renderer_destroy(pt_renderer* r);
+/* anyhow error text of the last failed call on this handle. */
+const char* pt_renderer_last_error(const pt_renderer* r);
+
+/* HalaRenderer::set_scene (src/bin/hala-pathtracer.rs:198): uploads geometry,
+ * materials, lights and cameras. The BVH is built on the device at commit. */
+pt_status pt_renderer_set_scene(pt_renderer* r, const pt_scene_desc* scene);
+/* HalaRenderer::set_envmap (src/bin/hala-pathtracer.rs:203): equirectangular
+ * RGB32F pixels (row 0 = theta 0) and the hdri_rotation in degrees. */
+pt_status pt_renderer_set_envmap(pt_renderer* r, const float* rgb, uint32_t width,
+                                 uint32_t height, float rotation_degrees);
+/* HalaRenderer::set_ground_color / set_sky_color (src/bin/hala-pathtracer.rs:205-206). */
+pt_status pt_renderer_set_ground_color(pt_renderer* r, const float rgba[4]);
+pt_status pt_renderer_set_sky_color(pt_renderer* r, const float rgba[4]);
+/* HalaRenderer::set_env_intensity (src/bin/hala-pathtracer.rs:208). */
+pt_status pt_renderer_set_env_intensity(pt_renderer* r, float intensity);
+/* HalaRenderer::set_exposure_value (src/bin/hala-pathtracer.rs:211). */
+pt_status pt_renderer_set_exposure_value(pt_renderer* r, float ev);
+/* MainUBO.camera_index (inc/global.glsl:16). */
+pt_status pt_renderer_set_camera_index(pt_renderer* r, uint32_t index);
+/* HalaRenderer::commit (src/bin/hala-pathtracer.rs:213): picks the feature
+ * permutation (src/bin/hala-pathtracer.rs:101-114), builds the BVH on the
+ * device and the environment alias tables. */
+pt_status pt_renderer_commit(pt_renderer* r);
+/* HalaRenderer::update + render (src/bin/hala-pathtracer.rs:264-285):
+ * traces `frames` progressive frames of one sample per pixel each and
+ * accumulates them (pathtracer.rgen.glsl:259-304). Stops at max_samples. */
+pt_status pt_renderer_render(pt_renderer* r, uint32_t frames);
+/* Restart accumulation at frame 0. */
+pt_status pt_renderer_reset(pt_renderer* r);
+/* Device->host copy of one image (the data HalaRenderer::save_images writes,
+ * src/bin/hala-pathtracer.rs:251). `bytes` must equal the image size. */
+pt_status pt_renderer_read_image(pt_renderer* r, pt_image which, void* host, size_t bytes);
+/* HalaRenderer::save_images (src/bin/hala-pathtracer.rs:251): writes
+ * <prefix>_color.pfm, <prefix>_albedo.pfm, <prefix>_normal.pfm (the files
+ * denoise.py:11-19 expects) and <prefix>_final.ppm. */
+pt_status pt_renderer_save_images(pt_renderer* r, const char* prefix);
+/* HalaRenderer::wait_idle (src/bin/hala-pathtracer.rs:228). */
+pt_status pt_renderer_wait_idle(pt_renderer* r);
+pt_status pt_renderer_get_stats(const pt_renderer* r, pt_stats* out);
+/* The CUDA stream (cudaStream_t) the renderer launches on, for event timing. */
+pt_status pt_renderer_get_stream(const pt_renderer* r, void** stream);
+
+/* ---- geometry queries on the committed scene ------------------------------
+ * Replaces traceRayEXT (pathtracer.rgen.glsl:56-68 closest hit,
+ * inc/lighting.glsl:119-130 shadow any-hit) for testing and external use.
+ * rays: n x 8 floats (origin xyz, tmin, direction xyz, tmax).
+ * hits: n x 4 words (t as float, u, v as float, id as uint32). id is the
+ * global triangle index, 0x80000000|light for an analytic light,
+ * 0xFFFFFFFF for a miss. For any_hit, only t/id are meaningful (id != miss
+ * means occluded). brute_force = 1 tests every primitive (no BVH). */
+pt_status pt_renderer_trace_rays(pt_renderer* r, const float* rays, uint32_t n,
+                                 int32_t any_hit, int32_t brute_force, uint32_t* hits);
+
+/* ---- helpers ------------------------------------------------------------- */
+
+/* Fills ax/ay from roughness/anisotropic the way the shaders expect them
+ * (inc/bxdf/disney.glsl:420, inc/bxdf/oren_nayar.glsl:35-46). */
+void pt_material_preprocess(pt_material* m);
+/* Default-initialised material (Disney-free diffuse white, opacity 1, ior 1.5,
+ * no maps, no medium). */
+void pt_material_default(pt_material* m);
+uint32_t pt_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HALA_PT_H */
