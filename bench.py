@@ -1,0 +1,303 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 wavefront path tracer (paths/s).
+
+One step = one complete render of the workload: W x H pixels x spp
+progressive frames through the full integrator (camera, closest hit,
+shading, next-event estimation, accumulation, tonemap). The default workload
+is the 9x9 Disney sphere grid under a 2048x1024 HDR sky, 1920x1080, 64 spp,
+depth 12, Russian roulette from depth 4, all synthetic.
+
+`value` is paths/s with the scene already resident in HBM (device time of the
+K timed renders, CUDA events on the renderer's stream). `e2e` is the same
+metric through the public API from host buffers: scene upload, BVH build,
+environment tables, the render and the image read-back are all inside its
+timed region.
+
+--impl reference times the CPU restatement of the reference integrator on
+the host cores over a bounded sample of the same workload.
+
+Multi-GPU: every rank renders its own full workload with a distinct sample
+range (independent units, no data-path collective): scaling "weak".
+"""
+import argparse
+import importlib
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "disney_grid_1080p_64spp": ("disney_grid", {}),
+    "cornell_256_16spp": ("cornell", {}),
+    "displaced_icosphere_1080p_32spp": ("displaced_icosphere", {}),
+    "media_box_1024_128spp": ("media_box", {}),
+}
+DEFAULT_WORKLOAD = "disney_grid_1080p_64spp"
+L2_FLUSH_BYTES = 256 << 20  # > 129 MB L2
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{gpu_index}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[3][k].lower().startswith("active")})
+        loaded = [r for r in rows if r[2] > 200.0] or rows
+        return {"sm_mhz": statistics.median(r[0] for r in loaded), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_baseline(scene, seconds=12.0, threads=0):
+    """The oracle (CPU restatement of the reference integrator) on the host
+    cores over a bounded, seeded sample of the workload's pixels."""
+    import numpy as np
+    from oracle import oracle
+    oracle.build()
+    o = oracle.Oracle(scene)
+    WH = scene.width * scene.height
+    rng = np.random.default_rng(1234)
+    probe = rng.choice(WH, size=min(WH, 2048), replace=False).astype(np.uint32)
+    t0 = time.perf_counter()
+    o.trace_paths(probe, 0, 1, threads)
+    rate = len(probe) / max(time.perf_counter() - t0, 1e-6)
+    want = max(2048.0, rate * seconds)
+    frames = int(min(scene.spp, max(1, math.ceil(want / WH))))
+    npix = int(min(WH, max(2048, want / frames)))
+    pix = rng.choice(WH, size=npix, replace=False).astype(np.uint32)
+    t0 = time.perf_counter()
+    o.trace_paths(pix, 0, frames, threads)
+    dt = time.perf_counter() - t0
+    cores = threads if threads > 0 else (os.cpu_count() or 1)
+    return {"value": npix * frames / dt, "unit": "paths/s", "cores": cores, "kind": "port",
+            "sample": f"{npix} seeded random pixels x {frames} spp of the full workload ({dt:.1f} s)"}
+
+
+def run_reference(args, scene, workload):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    vals = []
+    for k in range(args.warmup + args.steps):
+        cb = cpu_baseline(scene, seconds=max(2.0, 20.0 / (args.warmup + args.steps)))
+        if k >= args.warmup:
+            vals.append(cb)
+    v = statistics.median(c["value"] for c in vals)
+    paths_step = scene.width * scene.height * scene.spp
+    line = {
+        "impl": "reference", "metric": "paths/s", "value": v, "unit": "paths/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * paths_step / v,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload,
+        "cpu_baseline": {"value": v, "unit": "paths/s", "cores": vals[0]["cores"], "kind": "port",
+                         "sample": vals[0]["sample"]},
+        "e2e": {"value": v, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+
+    scenes = importlib.import_module("hala-pathtracer_gb300.scenes")
+    fn, kw = WORKLOADS[args.workload]
+    scene = getattr(scenes, fn)(**kw)
+    workload = {"workload": args.workload, "width": scene.width, "height": scene.height, "spp": scene.spp,
+                "max_depth": scene.max_depth, "rr_depth": scene.rr_depth, "triangles": scene.num_triangles,
+                "paths_per_step": scene.width * scene.height * scene.spp}
+    if args.impl == "reference":
+        return run_reference(args, scene, workload)
+
+    import numpy as np
+    import torch
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    pt = importlib.import_module("hala-pathtracer_gb300")
+    abi = pt.abi
+    pt.build()
+
+    scene.seed = scene.seed + rank * 100003  # distinct sample range per rank
+    r = pt.renderer_for(scene)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # warm-up
+    for _ in range(args.warmup):
+        r.reset()
+        r.render(scene.spp)
+    # traversal work per closest-hit ray (counting kernels, outside the timed region)
+    r.set_profiling(abi.PROFILE_COUNT)
+    r.reset()
+    r.render(max(1, scene.spp // 8))
+    cs = r.stats()
+    nodes_per_ray = cs.trav_nodes / max(cs.closest_rays, 1)
+    tris_per_ray = cs.trav_tris / max(cs.closest_rays, 1)
+    r.set_profiling(abi.PROFILE_TRACE_TIMING)
+
+    clocks = ClockSampler(local)
+    barrier()
+    clocks.start()
+    step_ms, trace_ms, trace_launches, closest, shadow, launches = [], 0.0, 0, 0, 0, 0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        r.reset()
+        r.render(scene.spp)
+        st = r.stats()
+        step_ms.append(st.render_ms)
+        trace_ms += st.trace_ms
+        trace_launches += st.trace_launches
+        closest += st.closest_rays
+        shadow += st.shadow_rays
+        launches += st.kernel_launches
+    barrier()
+    clk = clocks.stop()
+    total_ms = sum(step_ms)
+    if ws > 1:
+        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    paths_step = scene.width * scene.height * scene.spp
+    value = ws * paths_step * args.steps / (total_ms / 1e3)
+    rays_per_s = ws * (closest + shadow) / (total_ms / 1e3)
+    r.set_profiling(0)
+
+    # end to end through the public API, host buffers in and images out
+    e2e_ms = []
+    h2d = sum(v.nbytes + i.nbytes for v, i, _, _ in scene.meshes) + 144 * len(scene.materials) + \
+        64 * len(scene.lights) + 64 * len(scene.cameras)
+    if scene.env_rgb is not None:
+        h2d += scene.env_rgb.shape[0] * scene.env_rgb.shape[1] * 16
+    d2h = scene.width * scene.height * (4 + 16)
+    for k in range(args.warmup + args.steps):
+        flush.zero_()
+        barrier()
+        t0 = time.perf_counter()
+        rr = pt.renderer_for(scene)
+        rr.render(scene.spp)
+        _img = rr.image(abi.IMAGE_FINAL)
+        _acc = rr.image(abi.IMAGE_ACCUM)
+        rr.close()
+        barrier()
+        if k >= args.warmup:
+            e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    e2e_total = sum(e2e_ms)
+    if ws > 1:
+        t = torch.tensor([e2e_total], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    e2e_value = ws * paths_step * args.steps / (e2e_total / 1e3)
+
+    # roofline of the closest-hit kernel (algorithmic bytes per traced ray)
+    bytes_per_ray = 32 + 16 + 64 * nodes_per_ray + 48 * tris_per_ray
+    avg_launch_ms = trace_ms / max(trace_launches, 1)
+    achieved = bytes_per_ray * closest / (trace_ms / 1e3) / 1e9 if trace_ms > 0 else 0.0
+    peak, peak_kind = _peaks()
+    line = {
+        "metric": "paths/s", "value": value, "unit": "paths/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": dict(workload, l2="flushed between steps (256 MiB write)", rays_per_s=rays_per_s,
+                       closest_rays_per_step=closest / args.steps, shadow_rays_per_step=shadow / args.steps),
+        "e2e": {"value": e2e_value, "unit": "paths/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e2e_total / args.steps},
+        "roofline": {"kernel": "k_trace (closest hit)", "bound": "hbm", "achieved": achieved, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "bytes_per_ray": bytes_per_ray, "nodes_per_ray": nodes_per_ray, "tris_per_ray": tris_per_ray,
+                     "avg_launch_ms": avg_launch_ms, "launches": trace_launches,
+                     "trace_share_of_step": trace_ms / max(total_ms, 1e-9)},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            line["cpu_baseline"] = cpu_baseline(scene)
+        except Exception as e:  # the checker is optional for the GPU number
+            line["cpu_baseline"] = {"error": str(e)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    r.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

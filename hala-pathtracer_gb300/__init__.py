@@ -155,6 +155,10 @@ class Renderer:
         self._check(self._lib.pt_renderer_get_stats(self._h, C.byref(s)))
         return s
 
+    def set_profiling(self, flags):
+        """abi.PROFILE_TRACE_TIMING | abi.PROFILE_COUNT, or 0."""
+        self._check(self._lib.pt_renderer_set_profiling(self._h, int(flags)))
+
     def stream(self):
         p = C.c_void_p()
         self._check(self._lib.pt_renderer_get_stream(self._h, C.byref(p)))

@@ -102,7 +102,13 @@ class Stats(C.Structure):
                 ("render_ms", C.c_double), ("trace_ms", C.c_double),
                 ("bvh_build_ms", C.c_double), ("bvh_nodes", C.c_uint64),
                 ("triangles", C.c_uint64), ("features", C.c_uint32),
-                ("max_bounces_seen", C.c_uint32)]
+                ("max_bounces_seen", C.c_uint32), ("trace_launches", C.c_uint64),
+                ("trav_nodes", C.c_uint64), ("trav_tris", C.c_uint64),
+                ("kernel_launches", C.c_uint64)]
+
+
+PROFILE_TRACE_TIMING = 1
+PROFILE_COUNT = 2
 
 
 def make_config(width, height, max_depth=8, rr_depth=0, enable_tonemap=True, enable_aces=True,
@@ -141,6 +147,7 @@ RENDERER_SIGNATURES = {
     "pt_renderer_wait_idle": (C.c_int, [C.c_void_p]),
     "pt_renderer_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     "pt_renderer_get_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "pt_renderer_set_profiling": (C.c_int, [C.c_void_p, C.c_uint32]),
     "pt_renderer_trace_rays": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_uint32,
                                          C.c_int32, C.c_int32, C.POINTER(C.c_uint32)]),
     "pt_material_preprocess": (None, [C.POINTER(Material)]),

@@ -109,6 +109,8 @@ struct pt_renderer {
   uint64_t keep_count = 0;
   uint64_t frame_index = 0;
   pt_stats stats{};
+  uint32_t profiling = 0;
+  std::vector<cudaEvent_t> tev;  // start/stop pairs around closest-hit launches
 };
 
 namespace {
@@ -230,7 +232,7 @@ pt_status ensure_wave(pt_renderer* r, uint32_t cap) {
   CK(r, r->q_dis.ensure(cap));
   CK(r, r->q_shadow.ensure(cap));
   CK(r, r->counters.ensure(2 * Q_COUNT));
-  CK(r, r->rays.ensure(2));
+  CK(r, r->rays.ensure(4));
   r->wave_cap = cap;
   PathState& P = r->P;
   P.rng = r->s_rng.p;
@@ -347,6 +349,7 @@ void pt_renderer_destroy(pt_renderer* r) {
   if (r->ev0) cudaEventDestroy(r->ev0);
   if (r->ev1) cudaEventDestroy(r->ev1);
   if (r->pinned) cudaFreeHost(r->pinned);
+  for (cudaEvent_t e : r->tev) cudaEventDestroy(e);
   cudaStream_t s = r->stream;
   delete r;
   if (s) cudaStreamDestroy(s);
@@ -564,11 +567,14 @@ pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) {
     CK(r, r->keep_hash.ensure(total));
     r->keep_count = total;
   }
-  CK(r, cudaMemsetAsync(r->rays.p, 0, 2 * sizeof(unsigned long long), st));
+  CK(r, cudaMemsetAsync(r->rays.p, 0, 4 * sizeof(unsigned long long), st));
   CK(r, cudaEventRecord(r->ev0, st));
   uint32_t* cnt0 = r->counters.p;
   uint32_t* cnt1 = r->counters.p + Q_COUNT;
   uint32_t max_bounces = 0;
+  size_t ntimed = 0;
+  uint64_t launches = 0;
+  const uint64_t per_bounce = (r->features & PT_FEATURE_MEDIUM) ? 4 : 5;  // trace, logic, 2 shades (, shadow)
   for (uint64_t off = 0; off < total; off += cap) {
     uint32_t n = (uint32_t)std::min<uint64_t>(cap, total - off);
     uint64_t g0 = g_start + off;
@@ -583,7 +589,21 @@ pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) {
       uint32_t* qnext = (b & 1) ? r->q_a.p : r->q_b.p;
       CK(r, cudaMemsetAsync(out, 0, Q_COUNT * sizeof(uint32_t), st));
       QueueSet Q{qin, in_cnt, qnext, r->q_logic.p, r->q_diff.p, r->q_dis.p, r->q_shadow.p, out, r->rays.p};
-      launch_bounce(r->view, r->P, Q, live, st);
+      const bool timing = (r->profiling & PT_PROFILE_TRACE_TIMING) != 0;
+      if (timing) {
+        while (r->tev.size() < 2 * (ntimed + 1)) {
+          cudaEvent_t e;
+          CK(r, cudaEventCreate(&e));
+          r->tev.push_back(e);
+        }
+        CK(r, cudaEventRecord(r->tev[2 * ntimed], st));
+      }
+      launch_trace(r->view, r->P, Q, live, (r->profiling & PT_PROFILE_COUNT) != 0, st);
+      if (timing) {
+        CK(r, cudaEventRecord(r->tev[2 * ntimed + 1], st));
+        ++ntimed;
+      }
+      launch_shade(r->view, r->P, Q, live, st);
       CK(r, cudaGetLastError());
       CK(r, cudaMemcpyAsync(r->pinned, out + Q_NEXT, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
       CK(r, cudaStreamSynchronize(st));
@@ -591,6 +611,7 @@ pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) {
     }
     if (live > 0) return fail(r, PT_ERR_TIMEOUT, "paths still alive after the bounce cap");
     max_bounces = std::max(max_bounces, b);
+    launches += 2 + per_bounce * b;  // camera + accumulate + bounces
     launch_accumulate(r->P, g0, n, WH, r->accum.p, r->albedo.p, r->normal.p,
                       r->cfg.keep_samples ? r->keep_rad.p : nullptr, r->cfg.keep_samples ? r->keep_hash.p : nullptr,
                       g_start, st);
@@ -600,7 +621,7 @@ pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) {
                   r->cfg.use_simple_aces, st);
   CK(r, cudaGetLastError());
   CK(r, cudaEventRecord(r->ev1, st));
-  unsigned long long rays[2] = {0, 0};
+  unsigned long long rays[4] = {0, 0, 0, 0};
   CK(r, cudaMemcpyAsync(rays, r->rays.p, sizeof(rays), cudaMemcpyDeviceToHost, st));
   CK(r, cudaStreamSynchronize(st));
   float ms = 0.0f;
@@ -612,6 +633,24 @@ pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) {
   r->stats.shadow_rays = rays[1];
   r->stats.render_ms = ms;
   r->stats.max_bounces_seen = max_bounces;
+  r->stats.trav_nodes = rays[2];
+  r->stats.trav_tris = rays[3];
+  r->stats.trace_launches = ntimed;
+  r->stats.kernel_launches = launches + 1;  // + finalize
+  double tms = 0.0;
+  for (size_t k = 0; k < ntimed; ++k) {
+    float e = 0.0f;
+    cudaEventElapsedTime(&e, r->tev[2 * k], r->tev[2 * k + 1]);
+    tms += e;
+  }
+  r->stats.trace_ms = tms;
+  return PT_OK;
+}
+
+pt_status pt_renderer_set_profiling(pt_renderer* r, uint32_t flags) {
+  if (!r) return PT_ERR_INVALID_ARG;
+  if (flags & ~(PT_PROFILE_TRACE_TIMING | PT_PROFILE_COUNT)) return fail(r, PT_ERR_INVALID_ARG, "unknown profiling flag");
+  r->profiling = flags;
   return PT_OK;
 }
 

@@ -525,6 +525,7 @@ __device__ __forceinline__ float3 disney_sample(uint4& rng, bool& ans, const Sha
   float cdf2 = cdf1 + p.metal_pr;
   float cdf3 = cdf2 + p.glass_pr;
   float r3 = rand1(rng);
+  // flags bits 8..10: sampled lobe (hash only; the state keeps the low byte)
   if (r3 < cdf0) {
     L = cosine_sample_hemisphere(r1, r2);
     flags = RAY_FLAGS_REFLECTION;
@@ -532,7 +533,7 @@ __device__ __forceinline__ float3 disney_sample(uint4& rng, bool& ans, const Sha
     float3 H = sample_ggx_vndf(V, ax, ay, r1, r2);
     if (H.z < 0.0f) H = -H;
     L = normalize(reflect3(-V, H));
-    flags = RAY_FLAGS_REFLECTION;
+    flags = RAY_FLAGS_REFLECTION | (1u << 8);
   } else if (r3 < cdf3) {
     float3 H = sample_ggx_vndf(V, ax, ay, r1, r2);
     float F = dielectric_fresnel(fabsf(dot(V, H)), s.eta);
@@ -540,16 +541,16 @@ __device__ __forceinline__ float3 disney_sample(uint4& rng, bool& ans, const Sha
     r3 = (r3 - cdf2) / (cdf3 - cdf2);
     if (r3 < F) {
       L = normalize(reflect3(-V, H));
-      flags = RAY_FLAGS_REFLECTION;
+      flags = RAY_FLAGS_REFLECTION | (2u << 8);
     } else {
       L = normalize(refract3(-V, H, s.eta));
-      flags = RAY_FLAGS_TRANSMISSION;
+      flags = RAY_FLAGS_TRANSMISSION | (3u << 8);
     }
   } else {
     float3 H = sample_gtr1(m.clearcoat_roughness, r1, r2);
     if (H.z < 0.0f) H = -H;
     L = normalize(reflect3(-V, H));
-    flags = RAY_FLAGS_REFLECTION;
+    flags = RAY_FLAGS_REFLECTION | (4u << 8);
   }
   L = to_world(s.tangent, s.bitangent, N, L);
   V = to_world(s.tangent, s.bitangent, N, V);

@@ -18,7 +18,7 @@ struct QueueSet {
   uint32_t* disney;
   uint32_t* shadow;
   uint32_t* counts;            // [Q_COUNT], zeroed at the start of the bounce
-  unsigned long long* rays;    // [0] closest rays, [1] shadow/transmittance rays
+  unsigned long long* rays;    // [0] closest rays, [1] shadow rays, [2] nodes, [3] triangle tests
 };
 
 int device_sm_count();
@@ -26,7 +26,9 @@ int device_sm_count();
 // pt_render.cu
 void launch_camera(const DevScene& S, const PathState& P, uint64_t g0, uint32_t n, uint32_t* q_active,
                    uint32_t* active_count, cudaStream_t st);
-void launch_bounce(const DevScene& S, const PathState& P, const QueueSet& Q, uint32_t max_items, cudaStream_t st);
+void launch_trace(const DevScene& S, const PathState& P, const QueueSet& Q, uint32_t max_items, bool count,
+                  cudaStream_t st);
+void launch_shade(const DevScene& S, const PathState& P, const QueueSet& Q, uint32_t max_items, cudaStream_t st);
 void launch_accumulate(const PathState& P, uint64_t g0, uint32_t n, uint32_t WH, float4* accum, float4* albedo,
                        float4* normal, float4* keep_rad, uint32_t* keep_hash, uint64_t keep_g0, cudaStream_t st);
 void launch_finalize(const float4* accum, uchar4* final_img, uint32_t WH, float ev, int enable, int aces, int simple,

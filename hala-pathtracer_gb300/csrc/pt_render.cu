@@ -110,13 +110,14 @@ __global__ void k_camera(const __grid_constant__ DevScene S, PathState P, uint64
 }
 
 // ------------------------------------------------------------------ trace
-template <bool BRUTE>
+template <bool BRUTE, bool COUNT>
 __global__ void __launch_bounds__(256) k_trace(const __grid_constant__ DevScene S, PathState P, QueueSet Q) {
   const uint32_t n = *Q.in_count;
+  TravCount tc;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     uint32_t p = Q.in[i];
     float4 o4 = P.ray_o[p], d4 = P.ray_d[p];
-    HitRec h = trace_closest<BRUTE>(S, f3(o4), f3(d4), 0.0f, WORLD_SIZE);
+    HitRec h = trace_closest<BRUTE, COUNT>(S, f3(o4), f3(d4), 0.0f, WORLD_SIZE, &tc);
     P.hit[p] = make_float4(h.t, h.u, h.v, __uint_as_float(h.id));
     int cls = 0;  // 0 logic, 1 diffuse, 2 disney
     if (h.id != HIT_MISS && !(h.id & HIT_LIGHT_BIT)) {
@@ -127,6 +128,10 @@ __global__ void __launch_bounds__(256) k_trace(const __grid_constant__ DevScene 
     queue_push(Q.diffuse, &Q.counts[Q_DIFFUSE], p, cls == 1);
     queue_push(Q.disney, &Q.counts[Q_DISNEY], p, cls == 2);
     count_add(&Q.rays[0], 1u);
+  }
+  if (COUNT) {
+    atomicAdd(&Q.rays[2], (unsigned long long)tc.nodes);
+    atomicAdd(&Q.rays[3], (unsigned long long)tc.tris);
   }
 }
 
@@ -601,7 +606,7 @@ __global__ void __launch_bounds__(256) k_shade(const __grid_constant__ DevScene 
         float3 f = bsdf_sample<MAT>(sh.rng, ans, st.fr, mat, -d, st.ffnormal, L, pdf, sflags);
         d = L;
         state_pdf = pdf;
-        flags |= sflags;
+        flags |= sflags & 0xFFu;
         pend |= PEND_BSDF | (sflags << 8);
         if (state_pdf > 0.0f) {
           T *= f / state_pdf;
@@ -638,7 +643,7 @@ __global__ void __launch_bounds__(256) k_shade(const __grid_constant__ DevScene 
     // has to put the visibility events first
     bool deferred = !MEDIUM && (pend & (PEND_ENV | PEND_LIGHT));
     if (!deferred) {
-      if (pend & PEND_BSDF) hmix(sh.hash, 0x60000000u | ((pend >> 8) & 0xFFu));
+      if (pend & PEND_BSDF) hmix(sh.hash, 0x60000000u | ((pend >> 8) & 0xFFFu));
       if (pend & PEND_STOP) hmix(sh.hash, 0x61000000u);
       if (pend & PEND_RR) hmix(sh.hash, 0x72000000u);
     }
@@ -693,7 +698,7 @@ __global__ void __launch_bounds__(256) k_shadow(const __grid_constant__ DevScene
       hmix(hash, 0x50000000u | (occ ? 0u : 1u));
       if (!occ) Ld += f3(P.sh_c1[p]);
     }
-    if (pend & PEND_BSDF) hmix(hash, 0x60000000u | ((pend >> 8) & 0xFFu));
+    if (pend & PEND_BSDF) hmix(hash, 0x60000000u | ((pend >> 8) & 0xFFFu));
     if (pend & PEND_STOP) hmix(hash, 0x61000000u);
     if (pend & PEND_RR) hmix(hash, 0x72000000u);
     float3 rad = f3(r4) + f3(P.sh_T[p]) * Ld;
@@ -780,9 +785,15 @@ void launch_camera(const DevScene& S, const PathState& P, uint64_t g0, uint32_t 
   k_camera<<<(n + 255) / 256, 256, 0, st>>>(S, P, g0, n, q_active, active_count);
 }
 
-void launch_bounce(const DevScene& S, const PathState& P, const QueueSet& Q, uint32_t max_items, cudaStream_t st) {
+void launch_trace(const DevScene& S, const PathState& P, const QueueSet& Q, uint32_t max_items, bool count,
+                  cudaStream_t st) {
   int g = grid_for(max_items);
-  k_trace<false><<<g, 256, 0, st>>>(S, P, Q);
+  if (count) k_trace<false, true><<<g, 256, 0, st>>>(S, P, Q);
+  else k_trace<false, false><<<g, 256, 0, st>>>(S, P, Q);
+}
+
+void launch_shade(const DevScene& S, const PathState& P, const QueueSet& Q, uint32_t max_items, cudaStream_t st) {
+  int g = grid_for(max_items);
   k_shade_logic<<<g, 256, 0, st>>>(S, P, Q);
   const bool med = (S.features & PT_FEATURE_MEDIUM) != 0;
   const bool tr = (S.features & PT_FEATURE_TRANSPARENT) != 0;

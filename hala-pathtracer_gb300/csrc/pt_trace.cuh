@@ -141,8 +141,13 @@ constexpr int TRAV_STACK = 64;
 constexpr uint32_t TRAV_MAX_VISITS = 1u << 22;
 
 // Closest hit over triangles. Returns id == HIT_MISS when nothing is hit.
-template <bool BRUTE>
-__device__ __forceinline__ HitRec trace_tris_closest(const DevScene& S, float3 o, float3 d, float tmin, float tmax) {
+struct TravCount {
+  uint32_t nodes = 0, tris = 0;
+};
+
+template <bool BRUTE, bool COUNT = false>
+__device__ __forceinline__ HitRec trace_tris_closest(const DevScene& S, float3 o, float3 d, float tmin, float tmax,
+                                                     TravCount* tc = nullptr) {
   HitRec h;
   h.t = tmax;
   h.u = h.v = 0.0f;
@@ -167,6 +172,7 @@ __device__ __forceinline__ HitRec trace_tris_closest(const DevScene& S, float3 o
   for (;;) {
     while (cur >= 0) {
       if (++visits > TRAV_MAX_VISITS) return h;
+      if (COUNT) tc->nodes++;
       const float4* nd = S.nodes + 4 * cur;
       float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2);
       int4 n3 = __ldg(reinterpret_cast<const int4*>(nd + 3));
@@ -189,6 +195,7 @@ __device__ __forceinline__ HitRec trace_tris_closest(const DevScene& S, float3 o
     }
     // leaf
     uint32_t start = (uint32_t)cur & 0x03FFFFFFu, count = ((uint32_t)cur >> 26) & 0x1Fu;
+    if (COUNT) tc->tris += count;
     for (uint32_t s = start; s < start + count; ++s) {
       float4 a = __ldg(&S.tri[3 * s]), b = __ldg(&S.tri[3 * s + 1]), c = __ldg(&S.tri[3 * s + 2]);
       uint32_t id = __float_as_uint(a.w);
@@ -254,9 +261,10 @@ __device__ __forceinline__ bool trace_tris_any(const DevScene& S, float3 o, floa
 
 // Closest hit including the analytic light geometry. For a light hit,
 // u = light pdf (the hit attribute of lights.rint.glsl).
-template <bool BRUTE>
-__device__ __forceinline__ HitRec trace_closest(const DevScene& S, float3 o, float3 d, float tmin, float tmax) {
-  HitRec h = trace_tris_closest<BRUTE>(S, o, d, tmin, tmax);
+template <bool BRUTE, bool COUNT = false>
+__device__ __forceinline__ HitRec trace_closest(const DevScene& S, float3 o, float3 d, float tmin, float tmax,
+                                                TravCount* tc = nullptr) {
+  HitRec h = trace_tris_closest<BRUTE, COUNT>(S, o, d, tmin, tmax, tc);
   float lbest = (h.id != HIT_MISS) ? h.t : INF;
   for (uint32_t i = 0; i < S.num_lights; ++i) {
     float t, pdf;

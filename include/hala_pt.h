@@ -202,7 +202,15 @@ typedef struct pt_stats {
   uint64_t triangles;
   uint32_t features;         /* PT_FEATURE_* chosen at commit */
   uint32_t max_bounces_seen;
+  uint64_t trace_launches;   /* closest-hit kernel launches timed in the last render call */
+  uint64_t trav_nodes;       /* BVH nodes visited by closest-hit rays (PT_PROFILE_COUNT) */
+  uint64_t trav_tris;        /* triangle tests of closest-hit rays (PT_PROFILE_COUNT) */
+  uint64_t kernel_launches;  /* kernels launched by the last render call */
 } pt_stats;
+
+/* Profiling switches for pt_renderer_set_profiling. */
+#define PT_PROFILE_TRACE_TIMING 1u  /* CUDA events around every closest-hit launch */
+#define PT_PROFILE_COUNT 2u         /* count traversal work (slower counting kernels) */
 
 #define PT_FEATURE_MEDIUM 1u
 #define PT_FEATURE_VOL_MIS 2u
@@ -255,6 +263,9 @@ pt_status pt_renderer_save_images(pt_renderer* r, const char* prefix);
 /* HalaRenderer::wait_idle (src/bin/hala-pathtracer.rs:228). */
 pt_status pt_renderer_wait_idle(pt_renderer* r);
 pt_status pt_renderer_get_stats(const pt_renderer* r, pt_stats* out);
+/* Turns the PT_PROFILE_* instrumentation on or off (off by default). No
+ * counterpart in the reference, which has no GPU timers. */
+pt_status pt_renderer_set_profiling(pt_renderer* r, uint32_t flags);
 /* The CUDA stream (cudaStream_t) the renderer launches on, for event timing. */
 pt_status pt_renderer_get_stream(const pt_renderer* r, void** stream);
 

@@ -1231,6 +1231,8 @@ static V3 disney_sample(RNG& rng, bool& ans, const State& s, const Material& m, 
   float cdf2 = cdf1 + p.metal_pr;
   float cdf3 = cdf2 + p.glass_pr;
   float r3 = rand1(rng);
+  // flags bits 8..10 carry the sampled lobe (0 diffuse, 1 dielectric/metal,
+  // 2 glass reflection, 3 glass refraction, 4 clearcoat) for the path hash
   if (r3 < cdf0) {
     L = cosine_sample_hemisphere(r1, r2);
     flags = RAY_FLAGS_REFLECTION;
@@ -1238,7 +1240,7 @@ static V3 disney_sample(RNG& rng, bool& ans, const State& s, const Material& m, 
     V3 H = sample_ggx_vndf(V, ax, ay, r1, r2);
     if (H.z < 0.0f) H = -H;
     L = normalize(reflect(-V, H));
-    flags = RAY_FLAGS_REFLECTION;
+    flags = RAY_FLAGS_REFLECTION | (1u << 8);
   } else if (r3 < cdf3) {
     V3 H = sample_ggx_vndf(V, ax, ay, r1, r2);
     float F = dielectric_fresnel(std::fabs(dot(V, H)), s.eta);
@@ -1246,16 +1248,16 @@ static V3 disney_sample(RNG& rng, bool& ans, const State& s, const Material& m, 
     r3 = (r3 - cdf2) / (cdf3 - cdf2);
     if (r3 < F) {
       L = normalize(reflect(-V, H));
-      flags = RAY_FLAGS_REFLECTION;
+      flags = RAY_FLAGS_REFLECTION | (2u << 8);
     } else {
       L = normalize(refract(-V, H, s.eta));
-      flags = RAY_FLAGS_TRANSMISSION;
+      flags = RAY_FLAGS_TRANSMISSION | (3u << 8);
     }
   } else {
     V3 H = sample_gtr1(m.clearcoat_roughness, r1, r2);
     if (H.z < 0.0f) H = -H;
     L = normalize(reflect(-V, H));
-    flags = RAY_FLAGS_REFLECTION;
+    flags = RAY_FLAGS_REFLECTION | (4u << 8);
   }
   L = to_world(s.tangent, s.bitangent, N, L);
   V = to_world(s.tangent, s.bitangent, N, V);
@@ -1550,7 +1552,7 @@ struct Tracer {
           V3 f = bsdf_sample(rng, ans, st, mat, -ray.d, st.ffnormal, L, pdf, sflags);
           ray.d = L;
           st.pdf = pdf;
-          st.flags |= sflags;
+          st.flags |= sflags & 0xFFu;
           hmix(hash, 0x60000000u | sflags);
           if (st.pdf > 0.0f) {
             throughput *= f / st.pdf;

@@ -87,7 +87,9 @@ def test_per_path_radiance(pt, scenes, oracle_mod, name):
     err = np.abs(a - b)
     tol = REL_TOL * np.maximum(np.abs(a), np.abs(b)) + ABS_FLOOR
     bad = (err > tol).any(axis=1)
-    assert not bad.any(), f"{bad.sum()} agreeing paths differ; worst {err.max():.3g}"
+    idx = np.nonzero(agree)[0][bad][:5]
+    detail = "; ".join(f"path {k}: gpu {rad_g[k]} oracle {rad_o[k]}" for k in idx)
+    assert not bad.any(), f"{bad.sum()} agreeing paths differ; worst {err.max():.3g}; {detail}"
 
 
 def test_accumulated_images(pt, scenes, oracle_mod):
