@@ -109,6 +109,7 @@ class Stats(C.Structure):
 
 PROFILE_TRACE_TIMING = 1
 PROFILE_COUNT = 2
+NOALLOC_MAX_TRIANGLES = 65536
 
 
 def make_config(width, height, max_depth=8, rr_depth=0, enable_tonemap=True, enable_aces=True,
@@ -150,6 +151,9 @@ RENDERER_SIGNATURES = {
     "pt_renderer_set_profiling": (C.c_int, [C.c_void_p, C.c_uint32]),
     "pt_renderer_trace_rays": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_uint32,
                                          C.c_int32, C.c_int32, C.POINTER(C.c_uint32)]),
+    "pt_bvh_build_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
+                                       C.c_uint32, C.c_void_p, C.POINTER(C.c_uint32), C.c_void_p,
+                                       C.c_char_p, C.c_size_t]),
     "pt_material_preprocess": (None, [C.POINTER(Material)]),
     "pt_material_default": (None, [C.POINTER(Material)]),
     "pt_abi_version": (C.c_uint32, []),

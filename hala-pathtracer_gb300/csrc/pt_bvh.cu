@@ -10,6 +10,8 @@
 // writes the 64-byte traversal nodes and the triangles in leaf order.
 #include <cuda_runtime.h>
 
+#include <cstdio>
+#include <mutex>
 #include <vector>
 
 #include "pt_internal.h"
@@ -348,5 +350,146 @@ int build_bvh(const float4* tri_v0, const float4* tri_e1, const float4* tri_e2, 
   *num_nodes = nn;
   return 0;
 }
+
+
+// ---------------------------------------------------------------------------
+// Allocation-free build (pt_bvh_build_noalloc).
+//
+// Hosts that own all device memory themselves -- engines that reserve their
+// pools up front and may not call cudaMalloc/cudaFree inside the frame loop,
+// or code that must not touch the allocator while other work is being
+// recorded -- still need the per-frame BVH rebuild of animated geometry. For
+// them the build's scratch (bounds, centroids, id ping-pong buffers, task
+// lists, build nodes) lives in this file-scope device array instead of
+// cudaMalloc'ed memory. It holds the scratch of up to
+// PT_NOALLOC_MAX_TRIANGLES triangles (about 11.3 MB) and stays resident on
+// every device that loads the library until the process exits.
+namespace {
+
+constexpr size_t NA_MAX = PT_NOALLOC_MAX_TRIANGLES;
+constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+constexpr size_t NA_OFF_TLO = 0;
+constexpr size_t NA_OFF_THI = align256(NA_OFF_TLO + NA_MAX * sizeof(float4));
+constexpr size_t NA_OFF_TC = align256(NA_OFF_THI + NA_MAX * sizeof(float4));
+constexpr size_t NA_OFF_IDA = align256(NA_OFF_TC + NA_MAX * sizeof(float4));
+constexpr size_t NA_OFF_IDB = align256(NA_OFF_IDA + NA_MAX * sizeof(uint32_t));
+constexpr size_t NA_OFF_FIN = align256(NA_OFF_IDB + NA_MAX * sizeof(uint32_t));
+constexpr size_t NA_OFF_CNT = align256(NA_OFF_FIN + NA_MAX * sizeof(uint32_t));
+constexpr size_t NA_OFF_TKA = align256(NA_OFF_CNT + 4 * sizeof(uint32_t));
+constexpr size_t NA_OFF_TKB = align256(NA_OFF_TKA + (NA_MAX + 1) * sizeof(BuildTask));
+constexpr size_t NA_OFF_NOD = align256(NA_OFF_TKB + (NA_MAX + 1) * sizeof(BuildTask));
+constexpr size_t NA_BYTES = align256(NA_OFF_NOD + 2 * NA_MAX * sizeof(BuildNode));
+
+static __device__ __align__(256) unsigned char g_bvh_noalloc_scratch[NA_BYTES];
+
+// Device address of the scratch array, looked up once per device with that
+// device current. In host code the symbol itself is only a host-side stand-in.
+std::mutex g_na_mutex;
+void* g_na_ptr[64] = {};
+
+cudaError_t noalloc_scratch(unsigned char** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_na_mutex);
+  if (!g_na_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_bvh_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_na_ptr[dev] = p;
+  }
+  *out = static_cast<unsigned char*>(g_na_ptr[dev]);
+  return cudaSuccess;
+}
+
+pt_status na_fail(char* msg, size_t cap, pt_status st, const char* text) {
+  if (msg && cap) std::snprintf(msg, cap, "%s", text);
+  return st;
+}
+
+}  // namespace
+
+}  // namespace hpt
+
+extern "C" pt_status pt_bvh_build_noalloc(const void* tri_v0, const void* tri_e1, const void* tri_e2,
+                                          uint32_t num_triangles, void* nodes_out, uint32_t node_capacity,
+                                          void* tri_sorted_out, uint32_t* num_nodes_out, void* stream,
+                                          char* error_message, size_t error_capacity) {
+  using namespace hpt;
+  if (error_message && error_capacity) error_message[0] = '\0';
+  if (!num_nodes_out) return na_fail(error_message, error_capacity, PT_ERR_INVALID_ARG, "num_nodes_out is null");
+  *num_nodes_out = 0;
+  if (num_triangles > PT_NOALLOC_MAX_TRIANGLES) {
+    char buf[160];
+    std::snprintf(buf, sizeof(buf),
+                  "num_triangles %u exceeds the allocation-free limit of %u (PT_NOALLOC_MAX_TRIANGLES)",
+                  num_triangles, (unsigned)PT_NOALLOC_MAX_TRIANGLES);
+    return na_fail(error_message, error_capacity, PT_ERR_INVALID_ARG, buf);
+  }
+  if (num_triangles == 0) return PT_OK;
+  if (!tri_v0 || !tri_e1 || !tri_e2 || !nodes_out || !tri_sorted_out)
+    return na_fail(error_message, error_capacity, PT_ERR_INVALID_ARG, "a device pointer is null");
+  if (node_capacity < 2 * num_triangles)
+    return na_fail(error_message, error_capacity, PT_ERR_INVALID_ARG, "node_capacity must be >= 2 * num_triangles");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned char* base = nullptr;
+  cudaError_t e = noalloc_scratch(&base);
+  if (e != cudaSuccess) return na_fail(error_message, error_capacity, PT_ERR_CUDA, cudaGetErrorString(e));
+  const uint32_t n = num_triangles;
+  float4* tlo = reinterpret_cast<float4*>(base + NA_OFF_TLO);
+  float4* thi = reinterpret_cast<float4*>(base + NA_OFF_THI);
+  float4* tc = reinterpret_cast<float4*>(base + NA_OFF_TC);
+  uint32_t* ids_a = reinterpret_cast<uint32_t*>(base + NA_OFF_IDA);
+  uint32_t* ids_b = reinterpret_cast<uint32_t*>(base + NA_OFF_IDB);
+  uint32_t* final_ids = reinterpret_cast<uint32_t*>(base + NA_OFF_FIN);
+  uint32_t* counters = reinterpret_cast<uint32_t*>(base + NA_OFF_CNT);
+  BuildTask* tasks_a = reinterpret_cast<BuildTask*>(base + NA_OFF_TKA);
+  BuildTask* tasks_b = reinterpret_cast<BuildTask*>(base + NA_OFF_TKB);
+  BuildNode* nodes = reinterpret_cast<BuildNode*>(base + NA_OFF_NOD);
+  const float4* v0 = static_cast<const float4*>(tri_v0);
+  const float4* e1 = static_cast<const float4*>(tri_e1);
+  const float4* e2 = static_cast<const float4*>(tri_e2);
+  // The array keeps the previous call's contents: the root task and the
+  // counters are rewritten here; every other word is written before it is read.
+  k_prep<<<(n + 255) / 256, 256, 0, st>>>(v0, e1, e2, n, tlo, thi, tc, ids_a);
+  BuildTask root{0, 0, n, 0};
+  uint32_t init[4] = {1, 1, 0, 0};
+  cudaMemcpyAsync(tasks_a, &root, sizeof(root), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(counters, init, sizeof(init), cudaMemcpyHostToDevice, st);
+  uint32_t ntasks = 1;
+  BuildTask* cur = tasks_a;
+  BuildTask* nxt = tasks_b;
+  uint32_t* src = ids_a;
+  uint32_t* dst = ids_b;
+  int cur_slot = 1, nxt_slot = 2;
+  uint32_t host_count = 0;
+  for (int level = 0; level < 200 && ntasks > 0; ++level) {
+    cudaMemsetAsync(counters + nxt_slot, 0, sizeof(uint32_t), st);
+    k_level<<<ntasks, BUILD_THREADS, 0, st>>>(cur, counters + cur_slot, src, dst, final_ids, tlo, thi, tc, nodes,
+                                              counters, nxt, counters + nxt_slot);
+    cudaMemcpyAsync(&host_count, counters + nxt_slot, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return na_fail(error_message, error_capacity, PT_ERR_CUDA, cudaGetErrorString(e));
+    ntasks = host_count;
+    std::swap(cur, nxt);
+    std::swap(src, dst);
+    std::swap(cur_slot, nxt_slot);
+  }
+  if (ntasks != 0) return na_fail(error_message, error_capacity, PT_ERR_CUDA, "BVH build did not terminate");
+  uint32_t nn = 0;
+  cudaMemcpyAsync(&nn, counters, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return na_fail(error_message, error_capacity, PT_ERR_CUDA, cudaGetErrorString(e));
+  k_layout<<<(nn + 255) / 256, 256, 0, st>>>(nodes, nn, static_cast<float4*>(nodes_out));
+  k_reorder<<<(n + 255) / 256, 256, 0, st>>>(final_ids, n, v0, e1, e2, static_cast<float4*>(tri_sorted_out));
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return na_fail(error_message, error_capacity, PT_ERR_CUDA, cudaGetErrorString(e));
+  *num_nodes_out = nn;
+  return PT_OK;
+}
+
+namespace hpt {
 
 }  // namespace hpt

@@ -280,6 +280,37 @@ pt_status pt_renderer_get_stream(const pt_renderer* r, void** stream);
 pt_status pt_renderer_trace_rays(pt_renderer* r, const float* rays, uint32_t n,
                                  int32_t any_hit, int32_t brute_force, uint32_t* hits);
 
+/* ---- allocation-free BVH rebuild ------------------------------------------
+ * No counterpart in the reference (its acceleration structures are built by
+ * the Vulkan driver inside hala-renderer). Some callers may not call
+ * cudaMalloc or cudaFree while they run -- engines that reserve all device
+ * memory in their own pools at start-up and rebuild the BVH of animated
+ * geometry every frame without touching the allocator. This entry point builds
+ * the BVH of `num_triangles` world-space triangles into buffers the caller
+ * owns, with the build's scratch in a fixed library-owned device array.
+ *
+ *   tri_v0/e1/e2    device float4[num_triangles]: first vertex and the two edge
+ *                   vectors of each triangle (w ignored)
+ *   nodes_out       device float4[4 * node_capacity], node_capacity >= 2 * n
+ *   tri_sorted_out  device float4[3 * num_triangles]: triangles in leaf order
+ *                   (v0 with the input index in w's bits, e1, e2)
+ *   num_nodes_out   host: number of nodes written
+ *   stream          cudaStream_t (NULL = default stream)
+ *   error_message   optional host buffer for the reason of a failure
+ *
+ * Limits: at most PT_NOALLOC_MAX_TRIANGLES triangles (larger inputs return
+ * PT_ERR_INVALID_ARG with that reason); the scratch (about 11.3 MB) stays
+ * resident on every device that loads the library until the process exits.
+ * It calls no cudaMalloc/cudaFree. Its first call on a device looks up the
+ * scratch array's device address (cudaGetSymbolAddress); make that first call
+ * before any stream capture. All calls share the one array: calls that overlap
+ * on the GPU (other streams, other threads) race and must be serialised. */
+#define PT_NOALLOC_MAX_TRIANGLES 65536u
+pt_status pt_bvh_build_noalloc(const void* tri_v0, const void* tri_e1, const void* tri_e2,
+                               uint32_t num_triangles, void* nodes_out, uint32_t node_capacity,
+                               void* tri_sorted_out, uint32_t* num_nodes_out, void* stream,
+                               char* error_message, size_t error_capacity);
+
 /* ---- helpers ------------------------------------------------------------- */
 
 /* Fills ax/ay from roughness/anisotropic the way the shaders expect them
