@@ -35,9 +35,16 @@ def headers():
     return hs + [os.path.join(INCLUDE, "hala_pt.h")]
 
 
+# Shading code is compiled without multiply-add contraction so it rounds like
+# the CPU oracle (explicit fmaf calls are still fused).
+PER_FILE_FLAGS = {"pt_render.cu": ["-fmad=false"]}
+
+
 def _compile(src, verbose_ptxas=False):
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-    cmd = [nvcc()] + ARCH + NVCC_FLAGS + (["-Xptxas", "-v"] if verbose_ptxas else []) + ["-c", src, "-o", obj]
+    extra = PER_FILE_FLAGS.get(os.path.basename(src), [])
+    cmd = [nvcc()] + ARCH + NVCC_FLAGS + extra + (["-Xptxas", "-v"] if verbose_ptxas else []) + \
+        ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")

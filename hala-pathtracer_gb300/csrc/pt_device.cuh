@@ -2,8 +2,9 @@
 //
 // Every function restates the reference GLSL it names (paths relative to
 // shaders/src/ of hala-pathtracer). Operation order follows the GLSL so the
-// CPU oracle and this code round the same way wherever the math is plain
-// IEEE arithmetic; transcendental functions (sinf, expf, ...) are CUDA's.
+// CPU oracle and this code round the same way: plain IEEE arithmetic (this
+// code is compiled without FMA contraction), correctly rounded division and
+// square root, and the portable transcendental functions below.
 #pragma once
 #include <cstdint>
 
@@ -27,6 +28,134 @@ constexpr uint32_t RAY_FLAGS_IS_EMITTER = 0x2u;
 constexpr uint32_t RAY_FLAGS_SPECULAR = 0x4u;
 constexpr uint32_t RAY_FLAGS_REFLECTION = 0x8u;
 constexpr uint32_t RAY_FLAGS_TRANSMISSION = 0x10u;
+
+// ------------------------------------------------------------------ portable math
+// float32 sin/cos/tan/exp/log/pow/acos/atan2 with a fixed operation order
+// (explicit fused multiply-adds only): Cody-Waite argument reduction with
+// three-part constants, then polynomial kernels fitted by iteratively
+// reweighted least squares in relative error and rounded to float32. The CPU
+// oracle evaluates the same algorithm, so both round identically; accuracy
+// against 40-digit references: <= 1.5 ulp (sin, cos, exp, log, acos),
+// <= 2.6 ulp (tan, atan2), pow = exp(y log x) within GLSL's pow precision.
+constexpr float PM_TWO_OVER_PI = 0.6366197466850281f;
+constexpr float PM_PIO2_HI = 1.5707963705062866f, PM_PIO2_MID = -4.371138828673793e-08f,
+                PM_PIO2_LO = -1.7151245100058819e-15f;
+constexpr float PM_PIO4_HI = 0.7853981852531433f, PM_PIO4_MID = -2.1855694143368964e-08f;
+constexpr float PM_PI_HI = 3.1415927410125732f, PM_PI_MID = -8.742277657347586e-08f;
+constexpr float PM_LOG2E = 1.4426950216293335f;
+constexpr float PM_LN2_HI = 0.6931471824645996f, PM_LN2_MID = -1.9046542121259336e-09f;
+
+__device__ __forceinline__ void pm_sincos(float x, float& s, float& c) {
+  if (!(fabsf(x) <= 1.0e6f)) {
+    s = c = __int_as_float(0x7fc00000);
+    return;
+  }
+  float k = rintf(x * PM_TWO_OVER_PI);
+  float r = fmaf(-k, PM_PIO2_HI, x);
+  r = fmaf(-k, PM_PIO2_MID, r);
+  r = fmaf(-k, PM_PIO2_LO, r);
+  int q = (int)k;
+  float z = r * r;
+  float sp = fmaf(fmaf(fmaf(2.7249013783148257e-06f, z, -0.00019840076856780797f), z, 0.008333331905305386f), z,
+                  -0.1666666716337204f);
+  float sr = fmaf(r * z, sp, r);
+  float cp = fmaf(fmaf(fmaf(-2.730170649556385e-07f, z, 2.480060538800899e-05f), z, -0.00138888880610466f), z,
+                  0.0416666679084301f);
+  float cr = fmaf(z * z, cp, fmaf(-0.5f, z, 1.0f));
+  switch (q & 3) {
+    case 0: s = sr; c = cr; break;
+    case 1: s = cr; c = -sr; break;
+    case 2: s = -sr; c = -cr; break;
+    default: s = -cr; c = sr; break;
+  }
+}
+__device__ __forceinline__ float pm_sin(float x) { float s, c; pm_sincos(x, s, c); return s; }
+__device__ __forceinline__ float pm_cos(float x) { float s, c; pm_sincos(x, s, c); return c; }
+__device__ __forceinline__ float pm_tan(float x) { float s, c; pm_sincos(x, s, c); return s / c; }
+
+__device__ __forceinline__ float pm_exp(float x) {
+  if (x != x) return x;
+  if (x > 88.72283935546875f) return __int_as_float(0x7f800000);
+  if (x < -103.97208404541016f) return 0.0f;
+  float k = rintf(x * PM_LOG2E);
+  float r = fmaf(-k, PM_LN2_HI, x);
+  r = fmaf(-k, PM_LN2_MID, r);
+  float p = fmaf(fmaf(fmaf(fmaf(fmaf(0.00019924867956433445f, r, 0.0013933534501120448f), r, 0.008333264850080013f), r,
+                           0.041666463017463684f), r, 0.1666666716337204f), r, 0.5f);
+  float er = fmaf(r * r, p, r) + 1.0f;
+  int ki = (int)k;
+  int k1 = ki / 2, k2 = ki - k1;
+  return (er * __uint_as_float((uint32_t)(k1 + 127) << 23)) * __uint_as_float((uint32_t)(k2 + 127) << 23);
+}
+
+__device__ __forceinline__ float pm_log(float x) {
+  if (x != x || x < 0.0f) return __int_as_float(0x7fc00000);
+  if (x == 0.0f) return __int_as_float(0xff800000);
+  if (x == __int_as_float(0x7f800000)) return x;
+  int e = 0;
+  if (x < 1.17549435e-38f) {
+    x *= 8388608.0f;
+    e = -23;
+  }
+  uint32_t b = __float_as_uint(x);
+  e += (int)((b >> 23) & 0xffu) - 127;
+  float m = __uint_as_float((b & 0x007fffffu) | 0x3f800000u);
+  if (m > 1.41421356f) {
+    m *= 0.5f;
+    e += 1;
+  }
+  float f = m - 1.0f;
+  float s = f / (2.0f + f);
+  float z = s * s;
+  float p = fmaf(fmaf(fmaf(0.23334167897701263f, z, 0.28550657629966736f), z, 0.4000012278556824f), z,
+                 0.6666666865348816f);
+  float lm = fmaf(-s, fmaf(-z, p, f), f);
+  float fe = (float)e;
+  return fmaf(fe, PM_LN2_HI, fmaf(fe, PM_LN2_MID, lm));
+}
+
+__device__ __forceinline__ float pm_pow(float x, float y) {
+  if (y == 0.0f || x == 1.0f) return 1.0f;
+  if (x != x || y != y || x < 0.0f) return __int_as_float(0x7fc00000);
+  if (x == 0.0f) return y > 0.0f ? 0.0f : __int_as_float(0x7f800000);
+  return pm_exp(y * pm_log(x));
+}
+
+__device__ __forceinline__ float pm_asin_k(float x) {
+  float z = x * x;
+  float p = fmaf(fmaf(fmaf(fmaf(fmaf(0.034081507474184036f, z, 0.01690877228975296f), z, 0.031152866780757904f), z,
+                           0.044594623148441315f), z, 0.07500111311674118f), z, 0.1666666567325592f);
+  return fmaf(x * z, p, x);
+}
+__device__ __forceinline__ float pm_acos(float x) {
+  if (x != x || fabsf(x) > 1.0f) return __int_as_float(0x7fc00000);
+  if (fabsf(x) <= 0.5f) return PM_PIO2_HI - (pm_asin_k(x) - PM_PIO2_MID);
+  if (x > 0.0f) return 2.0f * pm_asin_k(sqrtf((1.0f - x) * 0.5f));
+  return PM_PI_HI - (2.0f * pm_asin_k(sqrtf((1.0f + x) * 0.5f)) - PM_PI_MID);
+}
+
+__device__ __forceinline__ float pm_atan_k(float t) {
+  float z = t * t;
+  float p = fmaf(fmaf(fmaf(fmaf(fmaf(0.05074314400553703f, z, -0.08635549992322922f), z, 0.11072912812232971f), z,
+                           -0.1428423672914505f), z, 0.19999979436397552f), z, -0.3333333432674408f);
+  return fmaf(t * z, p, t);
+}
+__device__ __forceinline__ float pm_atan2(float y, float x) {
+  if (x != x || y != y) return __int_as_float(0x7fc00000);
+  float ax = fabsf(x), ay = fabsf(y);
+  float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
+  float r;
+  if (mx == 0.0f) {
+    r = 0.0f;
+  } else {
+    float t = (mx == __int_as_float(0x7f800000)) ? (mn == mx ? 1.0f : 0.0f) : mn / mx;
+    if (t > 0.41421356f) r = PM_PIO4_HI + (pm_atan_k((t - 1.0f) / (t + 1.0f)) + PM_PIO4_MID);
+    else r = pm_atan_k(t);
+  }
+  if (ay > ax) r = (PM_PIO2_HI - r) + PM_PIO2_MID;
+  if (x < 0.0f) r = (PM_PI_HI - r) + PM_PI_MID;
+  return (y < 0.0f) ? -r : r;
+}
 
 // ------------------------------------------------------------------ float3
 __device__ __forceinline__ float3 f3(float s) { return make_float3(s, s, s); }
@@ -57,7 +186,7 @@ __device__ __forceinline__ float clampf(float x, float lo, float hi) { return fm
 __device__ __forceinline__ float3 clamp3(float3 v, float lo, float hi) {
   return make_float3(clampf(v.x, lo, hi), clampf(v.y, lo, hi), clampf(v.z, lo, hi));
 }
-__device__ __forceinline__ float3 vexp(float3 v) { return make_float3(expf(v.x), expf(v.y), expf(v.z)); }
+__device__ __forceinline__ float3 vexp(float3 v) { return make_float3(pm_exp(v.x), pm_exp(v.y), pm_exp(v.z)); }
 __device__ __forceinline__ float max3(float3 v) { return fmaxf(fmaxf(v.x, v.y), v.z); }
 __device__ __forceinline__ float smoothstepf(float e0, float e1, float x) {
   float t = clampf((x - e0) / (e1 - e0), 0.0f, 1.0f);
@@ -138,16 +267,16 @@ __device__ __forceinline__ float gtr1(float ndh, float a) {  // sampling.glsl:8-
   if (a >= 1.0f) return INV_PI;
   float a2 = a * a;
   float t = 1.0f + (a2 - 1.0f) * ndh * ndh;
-  return (a2 - 1.0f) / (PI * logf(a2) * t);
+  return (a2 - 1.0f) / (PI * pm_log(a2) * t);
 }
 // sampling.glsl:25-44 (y = sin*sin as the reference)
 __device__ __forceinline__ float3 sample_gtr1(float roughness, float r1, float r2) {
   float a = fmaxf(0.001f, roughness);
   float a2 = a * a;
   float phi = r1 * TWO_PI;
-  float ct = sqrtf((1.0f - powf(a2, 1.0f - r2)) / (1.0f - a2));
+  float ct = sqrtf((1.0f - pm_pow(a2, 1.0f - r2)) / (1.0f - a2));
   float st = clampf(sqrtf(1.0f - (ct * ct)), 0.0f, 1.0f);
-  float cp = cosf(phi);
+  float cp = pm_cos(phi);
   return make_float3(st * cp, st * st, ct);
 }
 // sampling.glsl:120-136
@@ -156,8 +285,8 @@ __device__ __forceinline__ float3 sample_ggx_vndf(float3 wi, float ax, float ay,
   float phi = (2.0f * r1 - 1.0f) * PI;
   float z = fmaf((1.0f - r2), (1.0f + wiStd.z), -wiStd.z);
   float sinTheta = sqrtf(clampf(1.0f - z * z, 0.0f, 1.0f));
-  float x = sinTheta * cosf(phi);
-  float y = sinTheta * sinf(phi);
+  float x = sinTheta * pm_cos(phi);
+  float y = sinTheta * pm_sin(phi);
   float3 wmStd = make_float3(x, y, z) + wiStd;
   return normalize(make_float3(wmStd.x * ax, wmStd.y * ay, wmStd.z));
 }
@@ -194,15 +323,15 @@ __device__ __forceinline__ float dielectric_fresnel(float cos_i, float eta) {
 __device__ __forceinline__ float3 cosine_sample_hemisphere(float r1, float r2) {
   float r = sqrtf(r1);
   float phi = TWO_PI * r2;
-  float x = r * cosf(phi);
-  float y = r * sinf(phi);
+  float x = r * pm_cos(phi);
+  float y = r * pm_sin(phi);
   float z = sqrtf(fmaxf(0.0f, 1.0f - x * x - y * y));
   return make_float3(x, y, z);
 }
 __device__ __forceinline__ float3 uniform_sample_hemisphere(float r1, float r2) {
   float r = sqrtf(fmaxf(0.0f, 1.0f - r1 * r1));
   float phi = TWO_PI * r2;
-  return make_float3(r * cosf(phi), r * sinf(phi), r1);
+  return make_float3(r * pm_cos(phi), r * pm_sin(phi), r1);
 }
 __device__ __forceinline__ float power_heuristic(float a, float b) {
   a *= a;
@@ -224,8 +353,8 @@ __device__ __forceinline__ float3 sample_hg(float3 V, float g, float r1, float r
   }
   float phi = r1 * TWO_PI;
   float st = clampf(sqrtf(1.0f - (ct * ct)), 0.0f, 1.0f);
-  float sp = sinf(phi);
-  float cp = cosf(phi);
+  float sp = pm_sin(phi);
+  float cp = pm_cos(phi);
   float3 v1, v2;
   onb(V, v1, v2);
   return st * cp * v1 + st * sp * v2 + ct * V;
@@ -239,7 +368,7 @@ __device__ __forceinline__ float phase_hg(float ct, float g) {
 // common/tonemap.glsl, common/common.glsl:26-39, pathtracer.rgen.glsl:280-301
 __device__ __forceinline__ float linear_2_srgb(float x) {
   if (x <= 0.0031308f) return 12.92f * x;
-  return 1.055f * powf(x, 1.0f / 2.4f) - 0.055f;
+  return 1.055f * pm_pow(x, 1.0f / 2.4f) - 0.055f;
 }
 __device__ __forceinline__ float3 aces_fitted(float3 c) {
   const float3 i0 = f3(0.59719f, 0.35458f, 0.04823f), i1 = f3(0.07600f, 0.90834f, 0.01566f),
@@ -258,7 +387,7 @@ __device__ __forceinline__ float3 aces_simple(float3 c) {
   return clamp3((c * (a * c + f3(b))) / (c * (y * c + f3(d)) + f3(e)), 0.0f, 1.0f);
 }
 __device__ __forceinline__ float3 finish_color(float3 c, float ev, bool enable, bool aces, bool simple) {
-  float exposure = powf(2.0f, ev);
+  float exposure = pm_pow(2.0f, ev);
   c = c * exposure;
   if (enable) {
     if (aces) c = simple ? aces_simple(c) : aces_fitted(c);
@@ -330,8 +459,8 @@ __device__ __forceinline__ float3 diffuse_sample(uint4& rng, bool& ans, const Sh
 
 // inc/bxdf/disney.glsl
 __device__ __forceinline__ float diffuse_directional_albedo(float th, float ax, float ay, float e0) {
-  return mixf(e0 + (1.0f - e0) * powf(fabsf(1.0f - th), 5.0f), 0.04762f + 0.95238f * e0,
-              1.0f - powf(fabsf(1.0f - ax * ay), 5.0f));
+  return mixf(e0 + (1.0f - e0) * pm_pow(fabsf(1.0f - th), 5.0f), 0.04762f + 0.95238f * e0,
+              1.0f - pm_pow(fabsf(1.0f - ax * ay), 5.0f));
 }
 __device__ __forceinline__ float coupled_diffuse(float ax, float ay, float wi, float wo, float e0) {
   float Ewi = diffuse_directional_albedo(wi, ax, ay, e0);
@@ -342,7 +471,7 @@ __device__ __forceinline__ float coupled_diffuse(float ax, float ay, float wi, f
 __device__ __forceinline__ float sheen_directional_albedo(float ct, float alpha) {
   float c = 1.0f - ct;
   float c3 = c * c * c;
-  return 0.65584461f * c3 + 1.0f / (4.16526551f + expf(-7.97291361f * sqrtf(alpha) + 6.33516894f));
+  return 0.65584461f * c3 + 1.0f / (4.16526551f + pm_exp(-7.97291361f * sqrtf(alpha) + 6.33516894f));
 }
 __device__ __forceinline__ float3 eval_disney_diffuse(float ax, float ay, float F0, const pt_material& m,
                                                       float3 c_sheen, float3 V, float3 L, float3 H, float& pdf) {
@@ -406,7 +535,7 @@ __device__ __forceinline__ float3 eval_microfacet_refraction(float ax, float ay,
   float eta2 = eta * eta;
   float jac = fabsf(ldh) / denom;
   pdf = G1 * fmaxf(0.0f, vdh) * D * jac / V.z;
-  return make_float3(powf(base.x, 0.5f), powf(base.y, 0.5f), powf(base.z, 0.5f)) * (f3(1.0f) - F) * D * G2 *
+  return make_float3(pm_pow(base.x, 0.5f), pm_pow(base.y, 0.5f), pm_pow(base.z, 0.5f)) * (f3(1.0f) - F) * D * G2 *
          fabsf(vdh) * jac * eta2 / fabsf(L.z * V.z);
 }
 __device__ __forceinline__ float3 eval_clearcoat(float ccr, float3 V, float3 L, float3 H, float& pdf) {

@@ -77,7 +77,7 @@ __global__ void k_camera(const __grid_constant__ DevScene S, PathState P, uint64
     d = normalize(f3(cam.forward));
     o = f3(cam.position) + f3(cam.right) * (dx * cam.fd_or_xmag) + f3(cam.up) * (dy * cam.ap_or_ymag);
   } else {
-    float scale = tanf(cam.yfov * 0.5f);
+    float scale = pm_tan(cam.yfov * 0.5f);
     dx *= scale * W / H;
     dy *= scale;
     float3 rd = normalize(f3(cam.right) * dx + f3(cam.up) * dy + f3(cam.forward));
@@ -87,7 +87,7 @@ __global__ void k_camera(const __grid_constant__ DevScene S, PathState P, uint64
       float3 focal = cam.fd_or_xmag * rd;
       float c1 = r.z * TWO_PI;
       float c2 = r.w * cam.ap_or_ymag;
-      float3 ap = (cosf(c1) * f3(cam.right) + sinf(c1) * f3(cam.up)) * sqrtf(c2);
+      float3 ap = (pm_cos(c1) * f3(cam.right) + pm_sin(c1) * f3(cam.up)) * sqrtf(c2);
       d = normalize(focal - ap);
       o = o + ap;
     }
@@ -152,7 +152,7 @@ __device__ __forceinline__ float3 env_texel(const DevScene& S, uint32_t idx) { r
 
 // inc/env_map.glsl:43-55
 __device__ __forceinline__ float env_pdf(const DevScene& S, float u, float v, float theta) {
-  float st = sinf(theta);
+  float st = pm_sin(theta);
   if (st > EPS) {
     float3 color = env_texel(S, env_texel_index(S, u, v)) * S.env_intensity;
     float pdf = luminance(color) / S.env_total_sum;
@@ -168,8 +168,8 @@ __device__ __forceinline__ float3 eval_env(const DevScene& S, float3 dir, uint32
     float a = fmaxf(dir.z, 0.0f);
     return mix(f3(S.ground), f3(S.sky), a) * S.env_intensity;
   }
-  float theta = acosf(dir.z);
-  float u = -(PI + atan2f(dir.y, dir.x)) * INV_TWO_PI - S.env_rotation;
+  float theta = pm_acos(dir.z);
+  float u = -(PI + pm_atan2(dir.y, dir.x)) * INV_TWO_PI - S.env_rotation;
   float v = theta * INV_PI;
   float mis = 1.0f;
   if (depth > 0 && (flags & RAY_FLAGS_SPECULAR) == 0) {
@@ -202,9 +202,9 @@ __device__ __forceinline__ float3 sample_env_map(const DevScene& S, uint4& rng, 
   pdf = luminance(color) / S.env_total_sum;
   float phi = (u + S.env_rotation) * TWO_PI;
   float theta = v * PI;
-  float st = sinf(theta);
+  float st = pm_sin(theta);
   if (st <= EPS) pdf = 0.0f;
-  float3 dir = normalize(make_float3(-st * cosf(phi), st * sinf(phi), cosf(theta)));
+  float3 dir = normalize(make_float3(-st * pm_cos(phi), st * pm_sin(phi), pm_cos(theta)));
   pdf = (pdf * (float)S.env_w * (float)S.env_h) / (TWO_PI * PI * st);
   return dir;
 }
@@ -239,8 +239,8 @@ __device__ __forceinline__ LightSample sample_light(uint4& rng, float3 fhp, cons
       float phi = TWO_PI * rand1(rng);
       float z = (1.0f - r * (1.0f - cos_alpha));
       float radius = sqrtf(1.0f - z * z);
-      float x = radius * cosf(phi);
-      float y = radius * sinf(phi);
+      float x = radius * pm_cos(phi);
+      float y = radius * pm_sin(phi);
       dir = to_world(T, B, N, make_float3(x, y, z));
     }
     o.normal = Lu;
@@ -525,7 +525,7 @@ __global__ void __launch_bounds__(256) k_shade(const __grid_constant__ DevScene 
       } else if (mtype == PT_MEDIUM_EMISSIVE) {
         rad += mcol * st.hit_distance * dens * T;
       } else {
-        float sd = fminf(-logf(rand1(sh.rng)) / dens, st.hit_distance);
+        float sd = fminf(-pm_log(rand1(sh.rng)) / dens, st.hit_distance);
         medium_sampled = sd < st.hit_distance;
         if (medium_sampled) {
           hmix(sh.hash, 0x70000001u);

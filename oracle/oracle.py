@@ -13,7 +13,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 SOURCES = [os.path.join(HERE, "pt_oracle.cpp")]
-HEADERS = [os.path.join(HERE, "pt_oracle.h"), os.path.join(HERE, "vec.h"),
+HEADERS = [os.path.join(HERE, "pt_oracle.h"), os.path.join(HERE, "vec.h"), os.path.join(HERE, "pmath.h"),
            os.path.join(HERE, "..", "include", "hala_pt.h")]
 
 
@@ -25,8 +25,12 @@ def build(force=False):
         if all(os.path.getmtime(s) <= mt for s in SOURCES + HEADERS):
             return LIB_PATH
     tmp = LIB_PATH + ".tmp"
+    import platform
+    # hardware fused multiply-add where the ISA needs a flag for it (x86-64);
+    # explicit std::fma only, no contraction of other expressions
+    isa = ["-mfma"] if platform.machine() in ("x86_64", "AMD64") else []
     cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
-           "-pthread", "-o", tmp] + SOURCES
+           "-pthread"] + isa + ["-o", tmp] + SOURCES
     subprocess.run(cmd, check=True)
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
@@ -75,6 +79,8 @@ def lib():
                                       C.c_uint32, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                       C.POINTER(C.c_uint32), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                       C.POINTER(C.c_float), C.POINTER(C.c_uint32)]),
+            "or_pmath": (None, [C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                C.c_uint32]),
             "or_tonemap": (None, [C.POINTER(C.c_float), C.c_float, C.c_int, C.c_int, C.c_int,
                                   C.POINTER(C.c_float)]),
         }
@@ -84,6 +90,15 @@ def lib():
             f.argtypes = a
         _lib = L
     return _lib
+
+
+def pmath(fn, x, y=None):
+    """Evaluates the oracle's portable float32 function `fn` (see or_pmath)."""
+    x = np.ascontiguousarray(x, np.float32)
+    y = np.ascontiguousarray(np.zeros_like(x) if y is None else y, np.float32)
+    out = np.empty_like(x)
+    lib().or_pmath(fn, _fp(x), _fp(y), _fp(out), len(x))
+    return out
 
 
 def _fp(a):

@@ -25,6 +25,7 @@
 #include <thread>
 #include <vector>
 
+#include "pmath.h"
 #include "vec.h"
 
 namespace orc {
@@ -129,18 +130,18 @@ inline float gtr1(float ndh, float a) {  // sampling.glsl:8-18
   if (a >= 1.0f) return INV_PI;
   float a2 = a * a;
   float t = 1.0f + (a2 - 1.0f) * ndh * ndh;
-  return (a2 - 1.0f) / (PI * std::log(a2) * t);
+  return (a2 - 1.0f) / (PI * pmath::log(a2) * t);
 }
 // sampling.glsl:25-44; the y component sin*sin is the reference's (kept).
 inline V3 sample_gtr1(float roughness, float r1, float r2) {
   float a = std::fmax(0.001f, roughness);
   float a2 = a * a;
   float phi = r1 * TWO_PI;
-  float ct = std::sqrt((1.0f - std::pow(a2, 1.0f - r2)) / (1.0f - a2));
+  float ct = std::sqrt((1.0f - pmath::pow(a2, 1.0f - r2)) / (1.0f - a2));
   float st = clampf(std::sqrt(1.0f - (ct * ct)), 0.0f, 1.0f);
-  float sp = std::sin(phi);
+  float sp = pmath::sin(phi);
   (void)sp;
-  float cp = std::cos(phi);
+  float cp = pmath::cos(phi);
   return V3(st * cp, st * st, ct);
 }
 // sampling.glsl:120-136 (spherical-cap VNDF)
@@ -149,8 +150,8 @@ inline V3 sample_ggx_vndf(V3 wi, float ax, float ay, float r1, float r2) {
   float phi = (2.0f * r1 - 1.0f) * PI;
   float z = std::fma((1.0f - r2), (1.0f + wiStd.z), -wiStd.z);
   float sinTheta = std::sqrt(clampf(1.0f - z * z, 0.0f, 1.0f));
-  float x = sinTheta * std::cos(phi);
-  float y = sinTheta * std::sin(phi);
+  float x = sinTheta * pmath::cos(phi);
+  float y = sinTheta * pmath::sin(phi);
   V3 c(x, y, z);
   V3 wmStd = c + wiStd;
   return normalize(V3(wmStd.x * ax, wmStd.y * ay, wmStd.z));
@@ -188,15 +189,15 @@ inline float dielectric_fresnel(float cos_i, float eta) {  // :218-236
 inline V3 cosine_sample_hemisphere(float r1, float r2) {  // :252-260
   float r = std::sqrt(r1);
   float phi = TWO_PI * r2;
-  float x = r * std::cos(phi);
-  float y = r * std::sin(phi);
+  float x = r * pmath::cos(phi);
+  float y = r * pmath::sin(phi);
   float z = std::sqrt(std::fmax(0.0f, 1.0f - x * x - y * y));
   return V3(x, y, z);
 }
 inline V3 uniform_sample_hemisphere(float r1, float r2) {  // :266-270
   float r = std::sqrt(std::fmax(0.0f, 1.0f - r1 * r1));
   float phi = TWO_PI * r2;
-  return V3(r * std::cos(phi), r * std::sin(phi), r1);
+  return V3(r * pmath::cos(phi), r * pmath::sin(phi), r1);
 }
 inline float power_heuristic(float a, float b) {  // :286-290
   a *= a;
@@ -218,8 +219,8 @@ inline V3 sample_hg(V3 V, float g, float r1, float r2) {  // :308-327
   }
   float phi = r1 * TWO_PI;
   float st = clampf(std::sqrt(1.0f - (ct * ct)), 0.0f, 1.0f);
-  float sp = std::sin(phi);
-  float cp = std::cos(phi);
+  float sp = pmath::sin(phi);
+  float cp = pmath::cos(phi);
   V3 v1, v2;
   onb(V, v1, v2);
   return st * cp * v1 + st * sp * v2 + ct * V;
@@ -233,7 +234,7 @@ inline float phase_hg(float ct, float g) {  // :333-336
 // common/tonemap.glsl, common/common.glsl:26-39
 inline float linear_2_srgb(float x) {
   if (x <= 0.0031308f) return 12.92f * x;
-  return 1.055f * std::pow(x, 1.0f / 2.4f) - 0.055f;
+  return 1.055f * pmath::pow(x, 1.0f / 2.4f) - 0.055f;
 }
 // v * mat3(c0, c1, c2) = (dot(v, c0), dot(v, c1), dot(v, c2))
 inline V3 aces_fitted(V3 c) {
@@ -257,7 +258,7 @@ inline V3 tonemap_lum(V3 c, float limit) { return c * 1.0f / (1.0f + luminance(c
 // pathtracer.rgen.glsl:280-301
 inline V3 finish_color(V3 accum, float ev, bool enable, bool aces, bool simple) {
   V3 c = accum;
-  float exposure = std::pow(2.0f, ev);
+  float exposure = pmath::pow(2.0f, ev);
   c = c * exposure;
   if (enable) {
     if (aces) c = simple ? aces_simple(c) : aces_fitted(c);
@@ -745,7 +746,7 @@ inline V3 env_texel(const Ctx& c, uint32_t idx) {
 
 // inc/env_map.glsl:43-55
 inline float env_pdf(const Ctx& c, float u, float v, float theta) {
-  float st = std::sin(theta);
+  float st = pmath::sin(theta);
   if (st > EPS) {
     V3 color = env_texel(c, env_texel_index(c, u, v)) * c.env_intensity;
     float pdf = luminance(color) / c.env_total_sum;
@@ -840,9 +841,9 @@ static V3 sample_env_map(const Ctx& c, RNG& rng, V3& color, float& pdf) {
   pdf = luminance(color) / c.env_total_sum;
   float phi = (u + c.env_rotation) * TWO_PI;
   float theta = v * PI;
-  float st = std::sin(theta);
+  float st = pmath::sin(theta);
   if (st <= EPS) pdf = 0.0f;
-  V3 dir = normalize(V3(-st * std::cos(phi), st * std::sin(phi), std::cos(theta)));
+  V3 dir = normalize(V3(-st * pmath::cos(phi), st * pmath::sin(phi), pmath::cos(theta)));
   pdf = (pdf * (float)c.env_w * (float)c.env_h) / (TWO_PI * PI * st);
   return dir;
 }
@@ -853,8 +854,8 @@ static V3 eval_env(const Ctx& c, V3 dir, uint32_t depth, uint32_t flags, float s
     float a = std::fmax(dir.z, 0.0f);
     return mix(c.ground, c.sky, a) * c.env_intensity;
   }
-  float theta = std::acos(dir.z);
-  float u = -(PI + std::atan2(dir.y, dir.x)) * INV_TWO_PI - c.env_rotation;
+  float theta = pmath::acos(dir.z);
+  float u = -(PI + pmath::atan2(dir.y, dir.x)) * INV_TWO_PI - c.env_rotation;
   float v = theta * INV_PI;
   float mis = 1.0f;
   if (depth > 0 && (flags & RAY_FLAGS_SPECULAR) == 0) {
@@ -895,8 +896,8 @@ static LightSample sample_light(RNG& rng, const State& s, const Light& L, uint32
         float phi = TWO_PI * rand1(rng);
         float z = (1.0f - r * (1.0f - cos_alpha));
         float radius = std::sqrt(1.0f - z * z);
-        float x = radius * std::cos(phi);
-        float y = radius * std::sin(phi);
+        float x = radius * pmath::cos(phi);
+        float y = radius * pmath::sin(phi);
         dir = to_world(T, B, N, V3(x, y, z));
       }
       o.normal = L.u;
@@ -1039,8 +1040,8 @@ inline void tint_colors(V3 base, float spec_tint, float sheen_tint, float eta, f
   c_sheen = mix(V3(1.0f), ctint, sheen_tint);
 }
 inline float diffuse_directional_albedo(float th, float ax, float ay, float e0) {  // :34-37
-  return mixf(e0 + (1.0f - e0) * std::pow(std::fabs(1.0f - th), 5.0f), 0.04762f + 0.95238f * e0,
-              1.0f - std::pow(std::fabs(1.0f - ax * ay), 5.0f));
+  return mixf(e0 + (1.0f - e0) * pmath::pow(std::fabs(1.0f - th), 5.0f), 0.04762f + 0.95238f * e0,
+              1.0f - pmath::pow(std::fabs(1.0f - ax * ay), 5.0f));
 }
 inline float diffuse_average_albedo(float ax, float ay, float e0) {  // :39-41
   return e0 + (-0.33263f * ax * ay - 0.072359f) * (1.0f - e0) * e0;
@@ -1054,7 +1055,7 @@ inline float coupled_diffuse(float ax, float ay, float wi, float wo, float e0) {
 inline float sheen_directional_albedo(float ct, float alpha) {  // :50-54
   float c = 1.0f - ct;
   float c3 = c * c * c;
-  return 0.65584461f * c3 + 1.0f / (4.16526551f + std::exp(-7.97291361f * std::sqrt(alpha) + 6.33516894f));
+  return 0.65584461f * c3 + 1.0f / (4.16526551f + pmath::exp(-7.97291361f * std::sqrt(alpha) + 6.33516894f));
 }
 inline V3 eval_disney_diffuse(float ax, float ay, float F0, float spec_tint, V3 base, float rough,
                               float subsurface, float sheen, V3 c_sheen, V3 V, V3 L, V3 H,
@@ -1121,7 +1122,7 @@ inline V3 eval_microfacet_refraction(float ax, float ay, V3 base, float eta, V3 
   float eta2 = eta * eta;
   float jac = std::fabs(ldh) / denom;
   pdf = G1 * std::fmax(0.0f, vdh) * D * jac / V.z;
-  return V3(std::pow(base.x, 0.5f), std::pow(base.y, 0.5f), std::pow(base.z, 0.5f)) * (V3(1.0f) - F) * D * G2 * std::fabs(vdh) * jac * eta2 / std::fabs(L.z * V.z);
+  return V3(pmath::pow(base.x, 0.5f), pmath::pow(base.y, 0.5f), pmath::pow(base.z, 0.5f)) * (V3(1.0f) - F) * D * G2 * std::fabs(vdh) * jac * eta2 / std::fabs(L.z * V.z);
 }
 inline V3 eval_clearcoat(float ccr, V3 V, V3 L, V3 H, float& pdf) {  // :229-252
   pdf = 0.0f;
@@ -1441,7 +1442,7 @@ struct Tracer {
       ray.o = cam.position + cam.right * (dx * cam.fd_or_xmag) + cam.up * (dy * cam.ap_or_ymag);
       return;
     }
-    float scale = std::tan(cam.yfov * 0.5f);
+    float scale = pmath::tan(cam.yfov * 0.5f);
     dx *= scale * W / Hh;
     dy *= scale;
     V3 rd = normalize(cam.right * dx + cam.up * dy + cam.forward);
@@ -1451,7 +1452,7 @@ struct Tracer {
       V3 focal = cam.fd_or_xmag * rd;
       float c1 = r[2] * TWO_PI;
       float c2 = r[3] * aperture;
-      V3 ap = (std::cos(c1) * cam.right + std::sin(c1) * cam.up) * std::sqrt(c2);
+      V3 ap = (pmath::cos(c1) * cam.right + pmath::sin(c1) * cam.up) * std::sqrt(c2);
       fd = normalize(focal - ap);
       fo = fo + ap;
     }
@@ -1517,7 +1518,7 @@ struct Tracer {
           } else if (st.medium.type == PT_MEDIUM_EMISSIVE) {
             radiance += st.medium.color * st.hit_distance * st.medium.density * throughput;
           } else {
-            float sd = std::fmin(-std::log(rand1(rng)) / st.medium.density, st.hit_distance);
+            float sd = std::fmin(-pmath::log(rand1(rng)) / st.medium.density, st.hit_distance);
             medium_sampled = sd < st.hit_distance;
             if (medium_sampled) {
               hmix(hash, 0x70000001u);
@@ -2031,6 +2032,21 @@ void or_bsdf_sample(int kind, const pt_material* m, const float tbn[9], float et
   *pdf_out = pdf;
   *flags_out = flags;
 }
+void or_pmath(int fn, const float* x, const float* y, float* out, uint32_t n) {
+  for (uint32_t i = 0; i < n; ++i) {
+    switch (fn) {
+      case 0: out[i] = pmath::sin(x[i]); break;
+      case 1: out[i] = pmath::cos(x[i]); break;
+      case 2: out[i] = pmath::tan(x[i]); break;
+      case 3: out[i] = pmath::exp(x[i]); break;
+      case 4: out[i] = pmath::log(x[i]); break;
+      case 5: out[i] = pmath::pow(x[i], y[i]); break;
+      case 6: out[i] = pmath::acos(x[i]); break;
+      default: out[i] = pmath::atan2(x[i], y[i]); break;
+    }
+  }
+}
+
 void or_tonemap(const float in[3], float ev, int enable, int aces, int simple, float out[3]) {
   V3 c = finish_color(v3(in), ev, enable != 0, aces != 0, simple != 0);
   out[0] = c.x; out[1] = c.y; out[2] = c.z;

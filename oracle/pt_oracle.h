@@ -73,6 +73,9 @@ void or_bsdf_eval(int kind, const pt_material* m, const float tbn[9], float eta,
 void or_bsdf_sample(int kind, const pt_material* m, const float tbn[9], float eta, uint32_t depth,
                     int any_non_specular, const float V[3], const float N[3], uint32_t s0[4],
                     float f_out[3], float L_out[3], float* pdf_out, uint32_t* flags_out);
+/* Portable float32 math of the oracle (oracle/pmath.h), for accuracy tests:
+ * fn 0 sin, 1 cos, 2 tan, 3 exp, 4 log, 5 pow(x, y), 6 acos, 7 atan2(y=x[i], x=y[i]). */
+void or_pmath(int fn, const float* x, const float* y, float* out, uint32_t n);
 /* Tonemap + exposure + sRGB of one linear colour (pathtracer.rgen.glsl:280-301). */
 void or_tonemap(const float in[3], float ev, int enable, int aces, int simple, float out[3]);
 

@@ -10,6 +10,8 @@
 #include <cmath>
 #include <cstdint>
 
+#include "pmath.h"
+
 namespace orc {
 
 struct V2 {
@@ -55,7 +57,7 @@ inline float clampf(float x, float lo, float hi) { return std::fmin(std::fmax(x,
 inline V3 clamp(V3 v, float lo, float hi) {
   return V3(clampf(v.x, lo, hi), clampf(v.y, lo, hi), clampf(v.z, lo, hi));
 }
-inline V3 vexp(V3 v) { return V3(std::exp(v.x), std::exp(v.y), std::exp(v.z)); }
+inline V3 vexp(V3 v) { return V3(pmath::exp(v.x), pmath::exp(v.y), pmath::exp(v.z)); }
 inline V3 vsqrt(V3 v) { return V3(std::sqrt(v.x), std::sqrt(v.y), std::sqrt(v.z)); }
 inline float max3(V3 v) { return std::fmax(std::fmax(v.x, v.y), v.z); }
 inline float smoothstepf(float e0, float e1, float x) {
