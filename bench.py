@@ -109,24 +109,24 @@ class ClockSampler:
 
 def cpu_baseline(scene, seconds=12.0, threads=0):
     """The oracle (CPU restatement of the reference integrator) on the host
-    cores over a bounded, seeded sample of the workload's pixels."""
+    cores over a bounded, seeded sample of the workload: a fixed set of
+    pixels rendered frame after frame (same RNG stream as the GPU) until
+    `seconds` of wall time have passed."""
     import numpy as np
     from oracle import oracle
     oracle.build()
     o = oracle.Oracle(scene)
     WH = scene.width * scene.height
     rng = np.random.default_rng(1234)
-    probe = rng.choice(WH, size=min(WH, 2048), replace=False).astype(np.uint32)
+    npix = min(WH, 1 << 17)
+    pix = np.sort(rng.choice(WH, size=npix, replace=False)).astype(np.uint32)
+    o.trace_paths(pix[:1024], 0, 1, threads)  # thread start-up, caches
+    frames, dt = 0, 0.0
     t0 = time.perf_counter()
-    o.trace_paths(probe, 0, 1, threads)
-    rate = len(probe) / max(time.perf_counter() - t0, 1e-6)
-    want = max(2048.0, rate * seconds)
-    frames = int(min(scene.spp, max(1, math.ceil(want / WH))))
-    npix = int(min(WH, max(2048, want / frames)))
-    pix = rng.choice(WH, size=npix, replace=False).astype(np.uint32)
-    t0 = time.perf_counter()
-    o.trace_paths(pix, 0, frames, threads)
-    dt = time.perf_counter() - t0
+    while dt < seconds and frames < scene.spp:
+        o.trace_paths(pix, frames, 1, threads)
+        frames += 1
+        dt = time.perf_counter() - t0
     cores = threads if threads > 0 else (os.cpu_count() or 1)
     return {"value": npix * frames / dt, "unit": "paths/s", "cores": cores, "kind": "port",
             "sample": f"{npix} seeded random pixels x {frames} spp of the full workload ({dt:.1f} s)"}
