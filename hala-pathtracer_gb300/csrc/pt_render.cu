@@ -193,12 +193,16 @@ __device__ __forceinline__ uint32_t alias_draw(const uint2* t, uint32_t n, float
 // inc/env_map.glsl:6-37, alias tables in place of the inverse-CDF textures
 __device__ __forceinline__ float3 sample_env_map(const DevScene& S, uint4& rng, float3& color, float& pdf) {
   float2 s = rand2(rng);
+  // v = marginal(s.x); u = conditional(s.y, v) on the row of texel v; colour
+  // = nearest texel at (u, v) (inc/env_map.glsl:7-12)
   float fv, fu;
-  uint32_t y = alias_draw(S.alias_rows, S.env_h, s.x, fv);
+  uint32_t yr = alias_draw(S.alias_rows, S.env_h, s.x, fv);
+  float v = ((float)yr + fv) / (float)S.env_h;
+  uint32_t y = (uint32_t)(v * (float)S.env_h);
+  if (y > S.env_h - 1) y = S.env_h - 1;
   uint32_t x = alias_draw(S.alias_cols + (size_t)y * S.env_w, S.env_w, s.y, fu);
-  float v = ((float)y + fv) / (float)S.env_h;
   float u = ((float)x + fu) / (float)S.env_w;
-  color = env_texel(S, y * S.env_w + x) * S.env_intensity;
+  color = env_texel(S, env_texel_index(S, u, v)) * S.env_intensity;
   pdf = luminance(color) / S.env_total_sum;
   float phi = (u + S.env_rotation) * TWO_PI;
   float theta = v * PI;

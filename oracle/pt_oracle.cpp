@@ -831,13 +831,18 @@ inline uint32_t alias_draw(const float* prob, const uint32_t* alias, uint32_t n,
 // inc/env_map.glsl:6-37 with alias tables in place of the inverse-CDF textures.
 static V3 sample_env_map(const Ctx& c, RNG& rng, V3& color, float& pdf) {
   V2 s = rand2(rng);
+  // v = marginal(s.x); u = conditional(s.y, v) on the row of texel v; the
+  // colour is the nearest texel at (u, v) -- inc/env_map.glsl:7-12 with the
+  // inverse-CDF textures realised as alias tables.
   float fv, fu;
-  uint32_t y = alias_draw(c.alias_prob_rows.data(), c.alias_idx_rows.data(), c.env_h, s.x, fv);
+  uint32_t yr = alias_draw(c.alias_prob_rows.data(), c.alias_idx_rows.data(), c.env_h, s.x, fv);
+  float v = ((float)yr + fv) / (float)c.env_h;
+  uint32_t y = (uint32_t)(v * (float)c.env_h);
+  if (y > c.env_h - 1) y = c.env_h - 1;
   uint32_t x = alias_draw(&c.alias_prob_cols[(size_t)y * c.env_w], &c.alias_idx_cols[(size_t)y * c.env_w],
                           c.env_w, s.y, fu);
-  float v = ((float)y + fv) / (float)c.env_h;
   float u = ((float)x + fu) / (float)c.env_w;
-  color = env_texel(c, y * c.env_w + x) * c.env_intensity;
+  color = env_texel(c, env_texel_index(c, u, v)) * c.env_intensity;
   pdf = luminance(color) / c.env_total_sum;
   float phi = (u + c.env_rotation) * TWO_PI;
   float theta = v * PI;

@@ -1,0 +1,93 @@
+"""Small scenes that pin the oracle and the GPU path to the reference's own
+shaders: every feature permutation (base, TRANSPARENT, MEDIUM+VOL_MIS,
+MEDIUM+VOL_MIS+TRANSPARENT), all five light types, sky and HDR environment,
+Lambert / Oren-Nayar / Disney (glass, metal, clearcoat, sheen), perspective,
+thin-lens and orthographic cameras, and every tonemap mode. Seed 0 (the
+reference seeds its RNG with the frame index only)."""
+import importlib
+
+S = importlib.import_module("hala-pathtracer_gb300.scenes")
+abi = S.abi
+
+
+def _cornell_base(w, h, spp):
+    s = S.cornell(w, h, spp, max_depth=6, rr_depth=2, seed=0)
+    return s
+
+
+def cornell():
+    return _cornell_base(24, 24, 3)
+
+
+def disney_ibl():
+    s = S.disney_grid(32, 18, 2, segments=12, rings=6, env_size=(64, 32))
+    s.env_rotation_deg = 77.8
+    s.env_intensity = 0.7
+    s.exposure_value = -1.0
+    return s
+
+
+def lights_icosphere():
+    s = S.displaced_icosphere(32, 18, 2, freq=6)
+    s.lights.append(S.directional_light((-0.2, 0.4, -0.9), (0.5, 0.5, 0.5), cone_deg=8.0))
+    s.lights.append(S.quad_light((-1.0, -1.5, 3.0), (0.6, 0, 0), (0, 0.6, 0), (6.0, 6.0, 6.0)))
+    s.materials[1].clearcoat = 0.8
+    s.materials[1].clearcoat_roughness = 0.2
+    s.materials[1].sheen = 0.5
+    s.materials[1].sheen_tint = 0.3
+    s.materials[1].specular_tint = 0.4
+    s.materials[1].subsurface = 0.3
+    s.materials[1].anisotropic = 0.5
+    S.preprocess_material(s.materials[1])
+    return s
+
+
+def media():
+    return S.media_box(24, 24, 2, max_depth=10, rr_depth=3, seed=0)
+
+
+def transparent():
+    s = _cornell_base(24, 24, 3)
+    panel = s.add_material(S.material((0.9, 0.8, 0.2), opacity=0.5))
+    s.add_mesh(*S.quad_mesh((0.2, 0.3, 0.1), (0.6, 0, 0), (0, 0, 0.6)), panel)
+    clear = s.add_material(S.material((0.5, 0.9, 0.6), opacity=0.0))
+    s.add_mesh(*S.quad_mesh((0.1, 0.8, 0.6), (0.3, 0, 0), (0, 0, 0.3)), clear)
+    return s
+
+
+def media_transparent():
+    s = S.media_box(24, 24, 2, max_depth=10, rr_depth=3, seed=0)
+    panel = s.add_material(S.material((0.8, 0.8, 0.8), opacity=0.6))
+    s.add_mesh(*S.quad_mesh((0.15, 0.4, 0.2), (0.7, 0, 0), (0, 0, 0.5)), panel)
+    return s
+
+
+def ortho_sky():
+    s = S.disney_grid(24, 16, 2, segments=10, rings=5, env_size=(8, 4))
+    s.env_rgb = None
+    s.ground_color = (0.2, 0.15, 0.1, 1.0)
+    s.sky_color = (0.4 * 4, 0.6 * 4, 0.9 * 4, 1.0)
+    s.cameras = [S.look_at((0.0, -9.0, 6.0), (0.0, 0.0, 0.0), 40.0, ortho=(5.0, 3.3))]
+    s.tonemap = (True, True, True)
+    return s
+
+
+def thin_lens_reinhard():
+    s = _cornell_base(24, 24, 3)
+    s.cameras = [S.look_at((0.5, -1.35, 0.5), (0.5, 0.5, 0.5), 40.0, aperture=0.02, focal_distance=1.8)]
+    s.tonemap = (True, False, False)
+    s.exposure_value = 0.5
+    return s
+
+
+def no_tonemap():
+    s = _cornell_base(16, 16, 2)
+    s.tonemap = (False, False, False)
+    return s
+
+
+PIN_SCENES = {
+    "cornell": cornell, "disney_ibl": disney_ibl, "lights_icosphere": lights_icosphere, "media": media,
+    "transparent": transparent, "media_transparent": media_transparent, "ortho_sky": ortho_sky,
+    "thin_lens_reinhard": thin_lens_reinhard, "no_tonemap": no_tonemap,
+}

@@ -110,3 +110,30 @@ def test_accumulated_images(pt, scenes, oracle_mod):
     for which in (0, 1, 2, 3):
         assert np.array_equal(r.image(which), o.image(which)), f"image {which} differs"
     assert r.stats().frame_index == sc.spp
+
+
+def _golden_scene_names():
+    import os
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    sys.path.insert(0, os.path.join(here, "golden"))
+    import pin_scenes
+    return sorted(pin_scenes.PIN_SCENES)
+
+
+@pytest.mark.parametrize("name", _golden_scene_names())
+def test_gpu_matches_reference_golden(pt, name):
+    """GPU images bit-identical to the reference's own shaders (golden fixtures)."""
+    import os
+    import pin_scenes
+    here = os.path.dirname(os.path.abspath(__file__))
+    g = np.load(os.path.join(here, "golden", f"ref_{name}.npz"))
+    sc = pin_scenes.PIN_SCENES[name]()
+    r = pt.renderer_for(sc)
+    r.render(int(g["frames"]))
+    for k, which in (("accum", 0), ("albedo", 1), ("normal", 2), ("final", 3)):
+        got = r.image(which)
+        if which == 3:
+            assert np.array_equal(got, g[k]), f"{name}: final image differs"
+        else:
+            assert np.array_equal(got.view(np.uint32), g[k].view(np.uint32)), f"{name}: {k} differs"
