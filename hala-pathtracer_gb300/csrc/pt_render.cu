@@ -776,12 +776,11 @@ __global__ void k_trace_rays(const __grid_constant__ DevScene S, const float4* r
 }
 
 // ------------------------------------------------------------------ launchers
+// One thread per queued item (the queue length is at most max_items): the
+// block scheduler then balances long and short traversals across SMs.
 static inline int grid_for(uint32_t max_items) {
-  int sms = device_sm_count();
   uint32_t want = (max_items + 255) / 256;
-  uint32_t cap = (uint32_t)sms * 8u;
-  if (want < 1) want = 1;
-  return (int)(want < cap ? want : cap);
+  return (int)(want < 1 ? 1 : want);
 }
 
 void launch_camera(const DevScene& S, const PathState& P, uint64_t g0, uint32_t n, uint32_t* q_active,

@@ -135,6 +135,15 @@ __device__ __forceinline__ void child_slabs(const float4 n0, const float4 n1, co
   h1 = tn1 <= tf1 * 1.0000005f;
 }
 
+// Reciprocal direction for the slab test. A component that is exactly zero
+// is replaced by +-1e-20 so fmaf(lo, inv, -o * inv) never forms inf - inf
+// (which would be NaN and cull boxes the ray passes through). Only culling
+// uses it; the triangle test keeps the true direction.
+__device__ __forceinline__ float3 slab_inv(float3 d) {
+  auto r = [](float x) { return 1.0f / (fabsf(x) < 1e-20f ? copysignf(1e-20f, x) : x); };
+  return make_float3(r(d.x), r(d.y), r(d.z));
+}
+
 constexpr int TRAV_STACK = 64;
 // Upper bound on node visits of one traversal; a well-formed tree never
 // reaches it, a corrupt one ends the traversal instead of looping.
@@ -164,7 +173,7 @@ __device__ __forceinline__ HitRec trace_tris_closest(const DevScene& S, float3 o
     return h;
   }
   if (S.num_tris == 0) return h;
-  float3 inv = make_float3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+  float3 inv = slab_inv(d);
   int32_t stack[TRAV_STACK];
   int sp = 0;
   int32_t cur = 0;  // root is always internal
@@ -220,7 +229,7 @@ __device__ __forceinline__ bool trace_tris_any(const DevScene& S, float3 o, floa
     return false;
   }
   if (S.num_tris == 0) return false;
-  float3 inv = make_float3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+  float3 inv = slab_inv(d);
   int32_t stack[TRAV_STACK];
   int sp = 0;
   int32_t cur = 0;

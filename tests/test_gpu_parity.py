@@ -57,6 +57,30 @@ def test_bvh_closest_bitexact(pt, scenes, oracle_mod, name):
     assert np.allclose(tf, to, rtol=1e-5)
 
 
+@pytest.mark.parametrize("name", ["cornell", "disney"])
+def test_bvh_axis_aligned_rays(pt, scenes, oracle_mod, name):
+    """Directions with exactly-zero components (orthographic cameras, walls)."""
+    sc = scenes.tiny_variants()[name]
+    r = pt.renderer_for(sc)
+    o = oracle_mod.Oracle(sc)
+    rng = np.random.default_rng(9)
+    lo, hi = _bounds(sc)
+    dirs = np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1],
+                     [0, 0.6, -0.8], [0.6, 0, 0.8], [-0.8, 0.6, 0], [0, -0.6, 0.8]], np.float32)
+    n = 3000
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, 0:3] = rng.uniform(lo, hi, size=(n, 3))
+    rays[:, 4:7] = dirs[rng.integers(0, len(dirs), n)]
+    rays[:, 7] = 1e4
+    hb = r.trace_rays(rays)
+    ho = o.trace_rays(rays, brute_force=True)
+    tri = (ho[:, 3] & 0x80000000) == 0
+    assert np.array_equal(hb[tri], ho[tri])
+    assert np.array_equal(hb[:, 3], ho[:, 3])
+    rays[:, 7] = rng.uniform(0.05, 2.0, n)
+    assert np.array_equal(r.trace_rays(rays, any_hit=True)[:, 3], o.trace_rays(rays, any_hit=True)[:, 3])
+
+
 @pytest.mark.parametrize("name", ["cornell", "icosphere"])
 def test_bvh_any_hit(pt, scenes, oracle_mod, name):
     sc = scenes.tiny_variants()[name]
