@@ -118,7 +118,7 @@ def cpu_baseline(scene, seconds=12.0, threads=0):
     o = oracle.Oracle(scene)
     WH = scene.width * scene.height
     rng = np.random.default_rng(1234)
-    npix = min(WH, 1 << 17)
+    npix = min(WH, 640 << 10)
     pix = np.sort(rng.choice(WH, size=npix, replace=False)).astype(np.uint32)
     o.trace_paths(pix[:1024], 0, 1, threads)  # thread start-up, caches
     frames, dt = 0, 0.0
@@ -156,6 +156,35 @@ def run_reference(args, scene, workload):
     return 0
 
 
+def serving_leg(n_jobs=256, rate=20.0, seed=0):
+    """The serving mix: `n_jobs` render jobs with Poisson arrivals at `rate`
+    jobs/s, scenes drawn from the four workloads with seed-perturbed
+    materials and lights, resolution log-uniform 128^2..1920x1080, spp
+    log-uniform 1..256, all through one pt_server."""
+    jm = importlib.import_module("hala-pathtracer_gb300.jobmix")
+    serve = importlib.import_module("hala-pathtracer_gb300.serve")
+    jobs = jm.job_mix(n_jobs=n_jobs, rate=rate, seed=seed)
+    with serve.Server() as srv:
+        # first launches of every kernel variant outside the measured mix
+        warm = jm.job_mix(n_jobs=8, rate=1000.0, seed=seed + 1, bases=jm.tiny_bases(), min_pixels=16 * 16,
+                          max_pixels=64 * 64, max_spp=2)
+        for j in warm:
+            srv.wait(srv.submit(j.scene, j.frames))
+        base = srv.stats()
+        res = jm.play(srv, jobs)
+        st = srv.stats()
+    res.update({
+        "arrival_rate_jobs_per_s": rate,
+        "wavefronts": st.wavefronts - base.wavefronts,
+        "device_busy_s": (st.busy_ms - base.busy_ms) / 1e3,
+        "rays_per_s": ((st.closest_rays - base.closest_rays) + (st.shadow_rays - base.shadow_rays)) /
+        max(res["span_s"], 1e-9),
+        "peak_resident_gb": st.peak_resident_bytes / 1e9,
+        "kernel_launches": st.kernel_launches - base.kernel_launches,
+    })
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -164,6 +193,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving mix")
+    ap.add_argument("--serving-jobs", type=int, default=256)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -291,9 +322,14 @@ def main():
             line["cpu_baseline"] = cpu_baseline(scene)
         except Exception as e:  # the checker is optional for the GPU number
             line["cpu_baseline"] = {"error": str(e)}
+    r.close()
+    if rank == 0 and ws == 1 and not args.no_serving:
+        try:
+            line["serving"] = serving_leg(n_jobs=args.serving_jobs)
+        except Exception as e:
+            line["serving"] = {"error": f"{type(e).__name__}: {e}"}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    r.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
     return 0

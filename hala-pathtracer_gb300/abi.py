@@ -107,6 +107,43 @@ class Stats(C.Structure):
                 ("kernel_launches", C.c_uint64)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_jobs", C.c_uint32),
+                ("wave_paths", C.c_uint32), ("quantum_paths", C.c_uint32),
+                ("use_graphs", C.c_uint32), ("fail_admission_of_job", C.c_uint64)]
+
+
+class JobDesc(C.Structure):
+    _fields_ = [("scene", C.POINTER(SceneDesc)), ("config", TracerConfig),
+                ("frames", C.c_uint32), ("camera_index", C.c_uint32),
+                ("env_rgb", C.POINTER(C.c_float)), ("env_width", C.c_uint32),
+                ("env_height", C.c_uint32), ("env_rotation_deg", C.c_float),
+                ("ground_color", C.c_float * 4), ("sky_color", C.c_float * 4),
+                ("env_intensity", C.c_float), ("exposure_value", C.c_float)]
+
+
+class JobInfo(C.Structure):
+    _fields_ = [("id", C.c_uint64), ("state", C.c_int32), ("status", C.c_int32),
+                ("paths_total", C.c_uint64), ("paths_done", C.c_uint64),
+                ("device_bytes", C.c_uint64), ("submit_ms", C.c_double),
+                ("admit_ms", C.c_double), ("done_ms", C.c_double), ("error", C.c_char * 128)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("jobs_submitted", C.c_uint64), ("jobs_done", C.c_uint64),
+                ("jobs_failed", C.c_uint64), ("jobs_cancelled", C.c_uint64),
+                ("jobs_rejected", C.c_uint64), ("jobs_queued", C.c_uint32),
+                ("jobs_running", C.c_uint32), ("resident_bytes", C.c_uint64),
+                ("peak_resident_bytes", C.c_uint64), ("wavefronts", C.c_uint64),
+                ("paths", C.c_uint64), ("closest_rays", C.c_uint64),
+                ("shadow_rays", C.c_uint64), ("kernel_launches", C.c_uint64),
+                ("graph_launches", C.c_uint64), ("busy_ms", C.c_double),
+                ("uptime_ms", C.c_double)]
+
+
+JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED, JOB_CANCELLED = range(5)
+JOB_STATE_NAMES = {0: "queued", 1: "running", 2: "done", 3: "failed", 4: "cancelled"}
+
 PROFILE_TRACE_TIMING = 1
 PROFILE_COUNT = 2
 NOALLOC_MAX_TRIANGLES = 65536
@@ -154,6 +191,17 @@ RENDERER_SIGNATURES = {
     "pt_bvh_build_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
                                        C.c_uint32, C.c_void_p, C.POINTER(C.c_uint32), C.c_void_p,
                                        C.c_char_p, C.c_size_t]),
+    "pt_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]),
+    "pt_server_destroy": (None, [C.c_void_p]),
+    "pt_server_last_error": (C.c_char_p, [C.c_void_p]),
+    "pt_server_submit": (C.c_int, [C.c_void_p, C.POINTER(JobDesc), C.POINTER(C.c_uint64)]),
+    "pt_server_poll": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(JobInfo)]),
+    "pt_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint32]),
+    "pt_server_read_image": (C.c_int, [C.c_void_p, C.c_uint64, C.c_int, C.c_void_p, C.c_size_t]),
+    "pt_server_cancel": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "pt_server_release": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "pt_server_pause": (C.c_int, [C.c_void_p, C.c_int32]),
+    "pt_server_get_stats": (C.c_int, [C.c_void_p, C.POINTER(ServerStats)]),
     "pt_material_preprocess": (None, [C.POINTER(Material)]),
     "pt_material_default": (None, [C.POINTER(Material)]),
     "pt_abi_version": (C.c_uint32, []),

@@ -13,7 +13,7 @@
 #include <string>
 #include <vector>
 
-#include "pt_internal.h"
+#include "pt_impl.h"
 
 namespace hpt {
 
@@ -27,91 +27,208 @@ int device_sm_count() {
   return sms;
 }
 
-template <class T>
-struct Buf {
-  T* p = nullptr;
-  size_t n = 0;
-  Buf() = default;
-  Buf(const Buf&) = delete;
-  Buf& operator=(const Buf&) = delete;
-  ~Buf() { release(); }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
+cudaError_t WaveBuffers::ensure(uint32_t want, bool want_med, bool want_multi) {
+  if (cap >= want && rng.p && (med || !want_med) && (multi || !want_multi)) return cudaSuccess;
+  want = std::max(want, cap);
+  want_med = want_med || (med && cap > 0);
+  want_multi = want_multi || (multi && cap > 0);
+  cap = 0;
+  cudaError_t e = cudaSuccess;
+  auto chk = [&](cudaError_t x) {
+    if (e == cudaSuccess) e = x;
+  };
+  chk(rng.ensure(want));
+  chk(ray_o.ensure(want));
+  chk(ray_d.ensure(want));
+  chk(hit.ensure(want));
+  chk(thr.ensure(want));
+  chk(rad.ensure(want));
+  chk(albedo.ensure(want));
+  chk(normal.ensure(want));
+  chk(depth.ensure(want));
+  chk(flags.ensure(want));
+  if (want_med) {
+    chk(med0.ensure(want));
+    chk(med1.ensure(want));
   }
-  cudaError_t ensure(size_t count) {
-    if (count <= n && p) return cudaSuccess;
-    release();
-    if (count == 0) return cudaSuccess;
-    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
-    if (e == cudaSuccess) n = count;
-    else p = nullptr;
-    return e;
+  if (want_multi) chk(job.ensure(want));
+  chk(sh_o.ensure(want));
+  chk(sh_d0.ensure(want));
+  chk(sh_d1.ensure(want));
+  chk(sh_c0.ensure(want));
+  chk(sh_c1.ensure(want));
+  chk(sh_T.ensure(want));
+  chk(q_a.ensure(want));
+  chk(q_b.ensure(want));
+  chk(q_logic.ensure(want));
+  chk(q_diff.ensure(want));
+  chk(q_dis.ensure(want));
+  chk(q_shadow.ensure(want));
+  chk(counters.ensure(2 * Q_COUNT));
+  chk(rays.ensure(4));
+  if (e != cudaSuccess) return e;
+  cap = want;
+  med = want_med;
+  multi = want_multi;
+  P.rng = rng.p;
+  P.ray_o = ray_o.p;
+  P.ray_d = ray_d.p;
+  P.hit = hit.p;
+  P.thr = thr.p;
+  P.rad = rad.p;
+  P.depth = depth.p;
+  P.flags = flags.p;
+  P.albedo = albedo.p;
+  P.normal = normal.p;
+  P.med0 = med ? med0.p : nullptr;
+  P.med1 = med ? med1.p : nullptr;
+  P.sh_o = sh_o.p;
+  P.sh_d0 = sh_d0.p;
+  P.sh_d1 = sh_d1.p;
+  P.sh_c0 = sh_c0.p;
+  P.sh_c1 = sh_c1.p;
+  P.sh_T = sh_T.p;
+  P.job = multi ? job.p : nullptr;
+  return cudaSuccess;
+}
+
+uint64_t WaveBuffers::bytes_per_path(bool med, bool multi) {
+  // rng 16, ray_o/ray_d/hit/thr/rad/albedo/normal 7x16, depth+flags 8,
+  // six NEE float4 96, six queues 24 (+ medium 24, + job slot 4)
+  return 16 + 7 * 16 + 8 + 96 + 24 + (med ? 24 : 0) + (multi ? 4 : 0);
+}
+
+cudaError_t run_bounces(const DevScene& S, WaveBuffers& W, uint32_t live, uint32_t max_depth, BounceLoop& L,
+                        uint32_t* pinned, cudaStream_t st) {
+  uint32_t* cnt0 = W.counters.p;
+  uint32_t* cnt1 = W.counters.p + Q_COUNT;
+  const uint32_t bounce_cap = 4u * max_depth + 4096u;
+  const bool timing = (L.profiling & PT_PROFILE_TRACE_TIMING) != 0 && L.tev;
+  uint32_t b = 0;
+  for (; b < bounce_cap && live > 0; ++b) {
+    uint32_t* out = (b & 1) ? cnt1 : cnt0;
+    uint32_t* in_cnt = ((b & 1) ? cnt0 : cnt1) + Q_NEXT;
+    uint32_t* qin = (b & 1) ? W.q_b.p : W.q_a.p;
+    uint32_t* qnext = (b & 1) ? W.q_a.p : W.q_b.p;
+    cudaError_t e = cudaMemsetAsync(out, 0, Q_COUNT * sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    QueueSet Q{qin, in_cnt, qnext, W.q_logic.p, W.q_diff.p, W.q_dis.p, W.q_shadow.p, out, W.rays.p};
+    if (timing) {
+      while (L.tev->size() < 2 * (L.ntimed + 1)) {
+        cudaEvent_t ev;
+        if ((e = cudaEventCreate(&ev)) != cudaSuccess) return e;
+        L.tev->push_back(ev);
+      }
+      if ((e = cudaEventRecord((*L.tev)[2 * L.ntimed], st)) != cudaSuccess) return e;
+    }
+    launch_trace(S, W.P, Q, live, (L.profiling & PT_PROFILE_COUNT) != 0, st);
+    if (timing) {
+      if ((e = cudaEventRecord((*L.tev)[2 * L.ntimed + 1], st)) != cudaSuccess) return e;
+      ++L.ntimed;
+    }
+    launch_shade(S, W.P, Q, live, st);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(pinned, out + Q_NEXT, sizeof(uint32_t), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+      return e;
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+    live = pinned[0];
   }
-};
+  L.bounces = b;
+  L.timed_out = live > 0;
+  return cudaSuccess;
+}
+
+pt_status validate_scene_desc(const pt_scene_desc* s, std::string* why) {
+  auto bad = [&](pt_status st, const char* m) {
+    if (why) *why = m;
+    return st;
+  };
+  if (!s) return bad(PT_ERR_INVALID_ARG, "scene is null");
+  if (s->num_cameras == 0 || !s->cameras) return bad(PT_ERR_INVALID_ARG, "scene has no camera");
+  if (s->num_cameras > PT_MAX_CAMERAS) return bad(PT_ERR_INVALID_ARG, "more than 8 cameras");
+  if (s->num_lights > PT_MAX_LIGHTS) return bad(PT_ERR_INVALID_ARG, "more than 16 lights");
+  if (s->num_primitives && !s->primitives) return bad(PT_ERR_INVALID_ARG, "primitives is null");
+  if (s->num_materials && !s->materials) return bad(PT_ERR_INVALID_ARG, "materials is null");
+  if (s->num_lights && !s->lights) return bad(PT_ERR_INVALID_ARG, "lights is null");
+  if (s->num_textures && !s->textures) return bad(PT_ERR_INVALID_ARG, "textures is null");
+  uint64_t nv = 0, nt = 0;
+  for (uint32_t i = 0; i < s->num_primitives; ++i) {
+    const pt_primitive& p = s->primitives[i];
+    if (p.num_indices % 3 != 0) return bad(PT_ERR_INVALID_ARG, "index count is not a multiple of 3");
+    if ((p.num_vertices && !p.vertices) || (p.num_indices && !p.indices))
+      return bad(PT_ERR_INVALID_ARG, "primitive arrays are null");
+    for (uint32_t k = 0; k < p.num_indices; ++k)
+      if (p.indices[k] >= p.num_vertices) return bad(PT_ERR_INVALID_ARG, "index out of range");
+    nv += p.num_vertices;
+    nt += p.num_indices / 3;
+  }
+  if (nt >= (1ull << 26) || nv >= (1ull << 31))
+    return bad(PT_ERR_UNSUPPORTED, "scene exceeds 2^26 triangles or 2^31 vertices");
+  return PT_OK;
+}
+
+pt_status validate_tracer_config(const pt_tracer_config* c, std::string* why) {
+  auto bad = [&](pt_status st, const char* m) {
+    if (why) *why = m;
+    return st;
+  };
+  if (!c) return bad(PT_ERR_INVALID_ARG, "config is null");
+  // src/config/window.rs:13-21 and src/config/tracer.rs:43-49
+  if (c->width == 0 || c->height == 0) return bad(PT_ERR_INVALID_ARG, "width and height must be positive");
+  if (c->rr_depth > c->max_depth) return bad(PT_ERR_INVALID_ARG, "rr_depth exceeds max_depth");
+  if ((uint64_t)c->width * c->height > (1ull << 31)) return bad(PT_ERR_UNSUPPORTED, "more than 2^31 pixels");
+  return PT_OK;
+}
+
+void renderer_drop_build_inputs(pt_renderer* r) {
+  r->raw_verts.release();
+  r->raw_idx.release();
+  r->dprims.release();
+  r->wpos.release();
+  r->tri_v0.release();
+  r->tri_e1.release();
+  r->tri_e2.release();
+}
+
+void renderer_drop_scene(pt_renderer* r) {
+  renderer_drop_build_inputs(r);
+  r->vnorm.release();
+  r->vtan.release();
+  r->vuv.release();
+  r->tri_sorted.release();
+  r->nodes.release();
+  r->tri_vidx.release();
+  r->tri_mat.release();
+  r->dmats.release();
+  r->env.release();
+  r->alias_rows.release();
+  r->alias_cols.release();
+  r->committed = false;
+  r->has_scene = false;
+}
+
+uint64_t renderer_estimate_bytes(const pt_scene_desc* d, uint32_t width, uint32_t height, uint32_t env_w,
+                                 uint32_t env_h) {
+  uint64_t nv = 0, nt = 0;
+  for (uint32_t i = 0; i < d->num_primitives; ++i) {
+    nv += d->primitives[i].num_vertices;
+    nt += d->primitives[i].num_indices / 3;
+  }
+  const uint64_t V = std::max<uint64_t>(nv, 1), T = std::max<uint64_t>(nt, 1);
+  // vertices: raw 44 + normal/tangent/position 48 + uv 8
+  // triangles: raw indices 12 + v0/e1/e2 48 + sorted 48 + 2 nodes 128 +
+  // vertex ids 12 + material 4; the BVH build's scratch is about 64 B more
+  uint64_t b = V * 100 + T * (252 + 64);
+  b += (uint64_t)d->num_materials * sizeof(pt_material) + 4096;
+  const uint64_t E = (uint64_t)env_w * env_h;
+  b += E * (16 + 8 + 16 + 8) + (uint64_t)env_h * 16;
+  b += (uint64_t)width * height * (3 * 16 + 4);
+  return b;
+}
 
 }  // namespace hpt
 
 using namespace hpt;
-
-struct pt_renderer {
-  pt_tracer_config cfg{};
-  cudaStream_t stream = nullptr;
-  std::string err;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  uint32_t* pinned = nullptr;
-
-  // scene
-  std::vector<pt_material> mats;
-  std::vector<pt_light> lights;
-  std::vector<pt_camera> cams;
-  uint32_t camera_index = 0;
-  uint32_t nverts = 0, ntris = 0, nnodes = 0;
-  bool has_scene = false, committed = false;
-  Buf<float> raw_verts;
-  Buf<uint32_t> raw_idx;
-  Buf<PrimUpload> dprims;
-  Buf<float4> vnorm, vtan, wpos, tri_v0, tri_e1, tri_e2, tri_sorted, nodes;
-  Buf<float2> vuv;
-  Buf<uint32_t> tri_vidx, tri_mat;
-  Buf<pt_material> dmats;
-
-  // environment
-  bool env_map = false;
-  uint32_t env_w = 0, env_h = 0;
-  float env_rotation = 0.0f, env_intensity = 1.0f;
-  float ground[4] = {0, 0, 0, 1}, sky[4] = {0, 0, 0, 1};
-  float exposure = 0.0f;
-  double env_total = 1.0;
-  Buf<float4> env;
-  Buf<uint2> alias_rows, alias_cols;
-
-  DevScene view{};
-  uint32_t features = 0;
-
-  // wavefront
-  uint32_t wave_cap = 0;
-  Buf<uint4> s_rng;
-  Buf<float4> s_ray_o, s_ray_d, s_hit, s_thr, s_rad, s_albedo, s_normal, s_med0;
-  Buf<float2> s_med1;
-  Buf<float4> s_sh_o, s_sh_d0, s_sh_d1, s_sh_c0, s_sh_c1, s_sh_T;
-  Buf<uint32_t> s_depth, s_flags;
-  Buf<uint32_t> q_a, q_b, q_logic, q_diff, q_dis, q_shadow, counters;
-  Buf<unsigned long long> rays;
-  PathState P{};
-
-  // images
-  Buf<float4> accum, albedo, normal;
-  Buf<uchar4> final_img;
-  Buf<float4> keep_rad;
-  Buf<uint32_t> keep_hash;
-  uint64_t keep_count = 0;
-  uint64_t frame_index = 0;
-  pt_stats stats{};
-  uint32_t profiling = 0;
-  std::vector<cudaEvent_t> tev;  // start/stop pairs around closest-hit launches
-};
 
 namespace {
 
@@ -202,60 +319,6 @@ void fill_view(pt_renderer* r) {
   S.features = r->features;
 }
 
-pt_status ensure_wave(pt_renderer* r, uint32_t cap) {
-  if (r->wave_cap >= cap && r->s_rng.p) return PT_OK;
-  const bool med = (r->features & PT_FEATURE_MEDIUM) != 0;
-  CK(r, r->s_rng.ensure(cap));
-  CK(r, r->s_ray_o.ensure(cap));
-  CK(r, r->s_ray_d.ensure(cap));
-  CK(r, r->s_hit.ensure(cap));
-  CK(r, r->s_thr.ensure(cap));
-  CK(r, r->s_rad.ensure(cap));
-  CK(r, r->s_albedo.ensure(cap));
-  CK(r, r->s_normal.ensure(cap));
-  CK(r, r->s_depth.ensure(cap));
-  CK(r, r->s_flags.ensure(cap));
-  if (med) {
-    CK(r, r->s_med0.ensure(cap));
-    CK(r, r->s_med1.ensure(cap));
-  }
-  CK(r, r->s_sh_o.ensure(cap));
-  CK(r, r->s_sh_d0.ensure(cap));
-  CK(r, r->s_sh_d1.ensure(cap));
-  CK(r, r->s_sh_c0.ensure(cap));
-  CK(r, r->s_sh_c1.ensure(cap));
-  CK(r, r->s_sh_T.ensure(cap));
-  CK(r, r->q_a.ensure(cap));
-  CK(r, r->q_b.ensure(cap));
-  CK(r, r->q_logic.ensure(cap));
-  CK(r, r->q_diff.ensure(cap));
-  CK(r, r->q_dis.ensure(cap));
-  CK(r, r->q_shadow.ensure(cap));
-  CK(r, r->counters.ensure(2 * Q_COUNT));
-  CK(r, r->rays.ensure(4));
-  r->wave_cap = cap;
-  PathState& P = r->P;
-  P.rng = r->s_rng.p;
-  P.ray_o = r->s_ray_o.p;
-  P.ray_d = r->s_ray_d.p;
-  P.hit = r->s_hit.p;
-  P.thr = r->s_thr.p;
-  P.rad = r->s_rad.p;
-  P.depth = r->s_depth.p;
-  P.flags = r->s_flags.p;
-  P.albedo = r->s_albedo.p;
-  P.normal = r->s_normal.p;
-  P.med0 = med ? r->s_med0.p : nullptr;
-  P.med1 = med ? r->s_med1.p : nullptr;
-  P.sh_o = r->s_sh_o.p;
-  P.sh_d0 = r->s_sh_d0.p;
-  P.sh_d1 = r->s_sh_d1.p;
-  P.sh_c0 = r->s_sh_c0.p;
-  P.sh_c1 = r->s_sh_c1.p;
-  P.sh_T = r->s_sh_T.p;
-  return PT_OK;
-}
-
 bool write_pfm(const char* path, const float4* px, uint32_t w, uint32_t h) {
   FILE* f = std::fopen(path, "wb");
   if (!f) return false;
@@ -316,10 +379,8 @@ void pt_material_preprocess(pt_material* m) {
 pt_status pt_renderer_create(const pt_tracer_config* cfg, pt_renderer** out) {
   if (!cfg || !out) return PT_ERR_INVALID_ARG;
   *out = nullptr;
-  // src/config/window.rs:13-21 and src/config/tracer.rs:43-49
-  if (cfg->width == 0 || cfg->height == 0) return PT_ERR_INVALID_ARG;
-  if (cfg->rr_depth > cfg->max_depth) return PT_ERR_INVALID_ARG;
-  if ((uint64_t)cfg->width * cfg->height > (1ull << 31)) return PT_ERR_UNSUPPORTED;
+  pt_status cs = validate_tracer_config(cfg, nullptr);
+  if (cs != PT_OK) return cs;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PT_ERR_CUDA;
   pt_renderer* r = new pt_renderer();
@@ -359,22 +420,15 @@ const char* pt_renderer_last_error(const pt_renderer* r) { return r ? r->err.c_s
 
 pt_status pt_renderer_set_scene(pt_renderer* r, const pt_scene_desc* s) {
   if (!r) return PT_ERR_INVALID_ARG;
-  if (!s) return fail(r, PT_ERR_INVALID_ARG, "scene is null");
-  if (s->num_cameras == 0 || !s->cameras) return fail(r, PT_ERR_INVALID_ARG, "scene has no camera");
-  if (s->num_cameras > PT_MAX_CAMERAS) return fail(r, PT_ERR_INVALID_ARG, "more than 8 cameras");
-  if (s->num_lights > PT_MAX_LIGHTS) return fail(r, PT_ERR_INVALID_ARG, "more than 16 lights");
-  if (s->num_primitives && !s->primitives) return fail(r, PT_ERR_INVALID_ARG, "primitives is null");
-  if (s->num_materials && !s->materials) return fail(r, PT_ERR_INVALID_ARG, "materials is null");
-  if (s->num_lights && !s->lights) return fail(r, PT_ERR_INVALID_ARG, "lights is null");
+  {
+    std::string why;
+    pt_status vs = validate_scene_desc(s, &why);
+    if (vs != PT_OK) return fail(r, vs, why);
+  }
   std::vector<PrimUpload> prims(s->num_primitives);
   uint64_t nv = 0, nt = 0;
   for (uint32_t i = 0; i < s->num_primitives; ++i) {
     const pt_primitive& p = s->primitives[i];
-    if (p.num_indices % 3 != 0) return fail(r, PT_ERR_INVALID_ARG, "index count is not a multiple of 3");
-    if ((p.num_vertices && !p.vertices) || (p.num_indices && !p.indices))
-      return fail(r, PT_ERR_INVALID_ARG, "primitive arrays are null");
-    for (uint32_t k = 0; k < p.num_indices; ++k)
-      if (p.indices[k] >= p.num_vertices) return fail(r, PT_ERR_INVALID_ARG, "index out of range");
     PrimUpload& u = prims[i];
     u.vbase = (uint32_t)nv;
     u.tbase = (uint32_t)nt;
@@ -387,8 +441,6 @@ pt_status pt_renderer_set_scene(pt_renderer* r, const pt_scene_desc* s) {
     nv += p.num_vertices;
     nt += p.num_indices / 3;
   }
-  if (nt >= (1ull << 26) || nv >= (1ull << 31))
-    return fail(r, PT_ERR_UNSUPPORTED, "scene exceeds 2^26 triangles or 2^31 vertices");
   r->committed = false;
   r->has_scene = false;
   r->nverts = (uint32_t)nv;
@@ -495,9 +547,7 @@ pt_status pt_renderer_commit(pt_renderer* r) {
     if (m.medium.type != PT_MEDIUM_NONE) f |= PT_FEATURE_MEDIUM | PT_FEATURE_VOL_MIS;
     if (m.opacity < 1.0f) f |= PT_FEATURE_TRANSPARENT;
   }
-  const bool wave_layout_changed = ((f ^ r->features) & PT_FEATURE_MEDIUM) != 0;
   r->features = f;
-  if (wave_layout_changed) r->wave_cap = 0;
   cudaStream_t st = r->stream;
   CK(r, r->nodes.ensure(4 * (size_t)std::max<uint32_t>(2 * r->ntris, 2)));
   CK(r, r->tri_sorted.ensure(3 * (size_t)std::max<uint32_t>(r->ntris, 1)));
@@ -557,9 +607,9 @@ pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) {
   if (total == 0) return PT_OK;
   uint64_t want = r->cfg.wave_paths ? r->cfg.wave_paths : (1u << 23);
   uint32_t cap = (uint32_t)std::min<uint64_t>(want, total);
-  pt_status ps = ensure_wave(r, std::max<uint32_t>(cap, r->wave_cap));
-  if (ps != PT_OK) return ps;
-  cap = std::max(cap, r->wave_cap);
+  const bool med = (r->features & PT_FEATURE_MEDIUM) != 0;
+  CK(r, r->W.ensure(cap, med, false));
+  cap = r->W.cap;
   cudaStream_t st = r->stream;
   const uint64_t g_start = r->frame_index * WH;
   if (r->cfg.keep_samples) {
@@ -567,62 +617,34 @@ pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) {
     CK(r, r->keep_hash.ensure(total));
     r->keep_count = total;
   }
-  CK(r, cudaMemsetAsync(r->rays.p, 0, 4 * sizeof(unsigned long long), st));
+  CK(r, cudaMemsetAsync(r->W.rays.p, 0, 4 * sizeof(unsigned long long), st));
   CK(r, cudaEventRecord(r->ev0, st));
-  uint32_t* cnt0 = r->counters.p;
-  uint32_t* cnt1 = r->counters.p + Q_COUNT;
   uint32_t max_bounces = 0;
-  size_t ntimed = 0;
   uint64_t launches = 0;
-  const uint64_t per_bounce = (r->features & PT_FEATURE_MEDIUM) ? 4 : 5;  // trace, logic, 2 shades (, shadow)
+  const uint64_t per_bounce = med ? 4 : 5;  // trace, logic, 2 shades (, shadow)
+  BounceLoop L;
+  L.profiling = r->profiling;
+  L.tev = &r->tev;
   for (uint64_t off = 0; off < total; off += cap) {
     uint32_t n = (uint32_t)std::min<uint64_t>(cap, total - off);
     uint64_t g0 = g_start + off;
-    launch_camera(r->view, r->P, g0, n, r->q_a.p, cnt1 + Q_NEXT, st);
-    uint32_t live = n;
-    uint32_t b = 0;
-    const uint32_t bounce_cap = 4u * r->cfg.max_depth + 4096u;
-    for (; b < bounce_cap && live > 0; ++b) {
-      uint32_t* out = (b & 1) ? cnt1 : cnt0;
-      uint32_t* in_cnt = ((b & 1) ? cnt0 : cnt1) + Q_NEXT;
-      uint32_t* qin = (b & 1) ? r->q_b.p : r->q_a.p;
-      uint32_t* qnext = (b & 1) ? r->q_a.p : r->q_b.p;
-      CK(r, cudaMemsetAsync(out, 0, Q_COUNT * sizeof(uint32_t), st));
-      QueueSet Q{qin, in_cnt, qnext, r->q_logic.p, r->q_diff.p, r->q_dis.p, r->q_shadow.p, out, r->rays.p};
-      const bool timing = (r->profiling & PT_PROFILE_TRACE_TIMING) != 0;
-      if (timing) {
-        while (r->tev.size() < 2 * (ntimed + 1)) {
-          cudaEvent_t e;
-          CK(r, cudaEventCreate(&e));
-          r->tev.push_back(e);
-        }
-        CK(r, cudaEventRecord(r->tev[2 * ntimed], st));
-      }
-      launch_trace(r->view, r->P, Q, live, (r->profiling & PT_PROFILE_COUNT) != 0, st);
-      if (timing) {
-        CK(r, cudaEventRecord(r->tev[2 * ntimed + 1], st));
-        ++ntimed;
-      }
-      launch_shade(r->view, r->P, Q, live, st);
-      CK(r, cudaGetLastError());
-      CK(r, cudaMemcpyAsync(r->pinned, out + Q_NEXT, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-      CK(r, cudaStreamSynchronize(st));
-      live = r->pinned[0];
-    }
-    if (live > 0) return fail(r, PT_ERR_TIMEOUT, "paths still alive after the bounce cap");
-    max_bounces = std::max(max_bounces, b);
-    launches += 2 + per_bounce * b;  // camera + accumulate + bounces
-    launch_accumulate(r->P, g0, n, WH, r->accum.p, r->albedo.p, r->normal.p,
+    launch_camera(r->view, r->W.P, g0, n, r->W.q_a.p, r->W.counters.p + Q_COUNT + Q_NEXT, st);
+    CK(r, run_bounces(r->view, r->W, n, r->cfg.max_depth, L, r->pinned, st));
+    if (L.timed_out) return fail(r, PT_ERR_TIMEOUT, "paths still alive after the bounce cap");
+    max_bounces = std::max(max_bounces, L.bounces);
+    launches += 2 + per_bounce * L.bounces;  // camera + accumulate + bounces
+    launch_accumulate(r->W.P, g0, n, WH, r->accum.p, r->albedo.p, r->normal.p,
                       r->cfg.keep_samples ? r->keep_rad.p : nullptr, r->cfg.keep_samples ? r->keep_hash.p : nullptr,
                       g_start, st);
     CK(r, cudaGetLastError());
   }
+  const size_t ntimed = L.ntimed;
   launch_finalize(r->accum.p, r->final_img.p, WH, r->exposure, r->cfg.enable_tonemap, r->cfg.enable_aces,
                   r->cfg.use_simple_aces, st);
   CK(r, cudaGetLastError());
   CK(r, cudaEventRecord(r->ev1, st));
   unsigned long long rays[4] = {0, 0, 0, 0};
-  CK(r, cudaMemcpyAsync(rays, r->rays.p, sizeof(rays), cudaMemcpyDeviceToHost, st));
+  CK(r, cudaMemcpyAsync(rays, r->W.rays.p, sizeof(rays), cudaMemcpyDeviceToHost, st));
   CK(r, cudaStreamSynchronize(st));
   float ms = 0.0f;
   cudaEventElapsedTime(&ms, r->ev0, r->ev1);

@@ -1,0 +1,140 @@
+// pt_impl.h -- host-side objects shared by the single-scene renderer
+// (pt_api.cu) and the job server (pt_serve.cu): device buffers, the
+// wavefront path state and the bounce loop that drives one wave.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "pt_internal.h"
+
+namespace hpt {
+
+template <class T>
+struct Buf {
+  T* p = nullptr;
+  size_t n = 0;
+  Buf() = default;
+  Buf(const Buf&) = delete;
+  Buf& operator=(const Buf&) = delete;
+  ~Buf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t ensure(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    release();
+    if (count == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    else p = nullptr;
+    return e;
+  }
+};
+
+// Structure-of-arrays state and queues of one wavefront of `cap` paths.
+// `med` adds the medium fields, `multi` the per-path job slot of a shared
+// wavefront.
+struct WaveBuffers {
+  uint32_t cap = 0;
+  bool med = false, multi = false;
+  Buf<uint4> rng;
+  Buf<float4> ray_o, ray_d, hit, thr, rad, albedo, normal, med0;
+  Buf<float2> med1;
+  Buf<float4> sh_o, sh_d0, sh_d1, sh_c0, sh_c1, sh_T;
+  Buf<uint32_t> depth, flags, job;
+  Buf<uint32_t> q_a, q_b, q_logic, q_diff, q_dis, q_shadow, counters;
+  Buf<unsigned long long> rays;
+  PathState P{};
+  cudaError_t ensure(uint32_t cap, bool med, bool multi);
+  // Bytes one path slot occupies (state + queues), for memory budgets.
+  static uint64_t bytes_per_path(bool med, bool multi);
+};
+
+// Options and results of the bounce loop of one wave.
+struct BounceLoop {
+  uint32_t profiling = 0;            // PT_PROFILE_* flags
+  std::vector<cudaEvent_t>* tev = nullptr;  // start/stop pairs around closest-hit launches
+  size_t ntimed = 0;
+  uint32_t bounces = 0;              // bounces run by the last wave
+  bool timed_out = false;            // paths still alive after the bounce cap
+};
+
+// Runs bounce after bounce of the `live` paths queued in W.q_a (the camera
+// kernel wrote their count to counters[Q_COUNT + Q_NEXT]) until no path
+// continues. The host reads the continuing-path count once per bounce
+// through `pinned` (one uint32_t of pinned host memory).
+cudaError_t run_bounces(const DevScene& S, WaveBuffers& W, uint32_t live, uint32_t max_depth, BounceLoop& L,
+                        uint32_t* pinned, cudaStream_t st);
+
+}  // namespace hpt
+
+struct pt_renderer {
+  pt_tracer_config cfg{};
+  cudaStream_t stream = nullptr;
+  std::string err;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  uint32_t* pinned = nullptr;
+
+  // scene
+  std::vector<pt_material> mats;
+  std::vector<pt_light> lights;
+  std::vector<pt_camera> cams;
+  uint32_t camera_index = 0;
+  uint32_t nverts = 0, ntris = 0, nnodes = 0;
+  bool has_scene = false, committed = false;
+  hpt::Buf<float> raw_verts;
+  hpt::Buf<uint32_t> raw_idx;
+  hpt::Buf<hpt::PrimUpload> dprims;
+  hpt::Buf<float4> vnorm, vtan, wpos, tri_v0, tri_e1, tri_e2, tri_sorted, nodes;
+  hpt::Buf<float2> vuv;
+  hpt::Buf<uint32_t> tri_vidx, tri_mat;
+  hpt::Buf<pt_material> dmats;
+
+  // environment
+  bool env_map = false;
+  uint32_t env_w = 0, env_h = 0;
+  float env_rotation = 0.0f, env_intensity = 1.0f;
+  float ground[4] = {0, 0, 0, 1}, sky[4] = {0, 0, 0, 1};
+  float exposure = 0.0f;
+  double env_total = 1.0;
+  hpt::Buf<float4> env;
+  hpt::Buf<uint2> alias_rows, alias_cols;
+
+  hpt::DevScene view{};
+  uint32_t features = 0;
+
+  // wavefront
+  hpt::WaveBuffers W;
+
+  // images
+  hpt::Buf<float4> accum, albedo, normal;
+  hpt::Buf<uchar4> final_img;
+  hpt::Buf<float4> keep_rad;
+  hpt::Buf<uint32_t> keep_hash;
+  uint64_t keep_count = 0;
+  uint64_t frame_index = 0;
+  pt_stats stats{};
+  uint32_t profiling = 0;
+  std::vector<cudaEvent_t> tev;  // start/stop pairs around closest-hit launches
+};
+
+namespace hpt {
+// Frees the build-time inputs of a committed scene (raw vertices, indices,
+// unsorted triangles): rendering needs only the flattened attributes, the
+// BVH and the sorted triangles.
+void renderer_drop_build_inputs(pt_renderer* r);
+// Frees everything of a finished render but its four images.
+void renderer_drop_scene(pt_renderer* r);
+// Checks of set_scene / HalaRenderer::new; `why` receives the reason.
+pt_status validate_scene_desc(const pt_scene_desc* desc, std::string* why);
+pt_status validate_tracer_config(const pt_tracer_config* config, std::string* why);
+// Device bytes a renderer for `desc` at width x height would hold after
+// commit (scene, BVH, environment tables, images), without wave buffers.
+uint64_t renderer_estimate_bytes(const pt_scene_desc* desc, uint32_t width, uint32_t height, uint32_t env_w,
+                                 uint32_t env_h);
+}  // namespace hpt

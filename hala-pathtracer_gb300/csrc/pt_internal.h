@@ -29,8 +29,11 @@ void launch_camera(const DevScene& S, const PathState& P, uint64_t g0, uint32_t 
 void launch_trace(const DevScene& S, const PathState& P, const QueueSet& Q, uint32_t max_items, bool count,
                   cudaStream_t st);
 void launch_shade(const DevScene& S, const PathState& P, const QueueSet& Q, uint32_t max_items, cudaStream_t st);
+void launch_camera_multi(const PathState& P, const WaveSegment* segs, uint32_t nseg, uint32_t n, uint32_t* q_active,
+                         uint32_t* active_count, cudaStream_t st);
 void launch_accumulate(const PathState& P, uint64_t g0, uint32_t n, uint32_t WH, float4* accum, float4* albedo,
-                       float4* normal, float4* keep_rad, uint32_t* keep_hash, uint64_t keep_g0, cudaStream_t st);
+                       float4* normal, float4* keep_rad, uint32_t* keep_hash, uint64_t keep_g0, cudaStream_t st,
+                       uint32_t wave_off = 0);
 void launch_finalize(const float4* accum, uchar4* final_img, uint32_t WH, float ev, int enable, int aces, int simple,
                      cudaStream_t st);
 void launch_trace_rays(const DevScene& S, const float4* rays, uint32_t n, int any_hit, int brute, uint4* hits,

@@ -49,12 +49,8 @@ __device__ __forceinline__ void count_add(unsigned long long* c, uint32_t v) {
 // ------------------------------------------------------------------ camera
 // perspective_ray.rcall.glsl:12-65, orthographic_ray.rcall.glsl:12-46,
 // state initialisation pathtracer.rgen.glsl:23-54
-__global__ void k_camera(const __grid_constant__ DevScene S, PathState P, uint64_t g0, uint32_t n,
-                         uint32_t* q_active, uint32_t* active_count) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+__device__ __forceinline__ void init_path(const DevScene& S, const PathState& P, uint32_t i, uint64_t g) {
   const uint64_t WH = (uint64_t)S.width * S.height;
-  uint64_t g = g0 + i;
   uint32_t pix = (uint32_t)(g % WH);
   uint32_t frame = (uint32_t)(g / WH);
   uint32_t px = pix % S.width, py = pix / S.width;
@@ -105,17 +101,44 @@ __global__ void k_camera(const __grid_constant__ DevScene S, PathState P, uint64
     P.med0[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     P.med1[i] = make_float2(1.0f, __uint_as_float(PT_MEDIUM_NONE));
   }
+}
+
+__global__ void k_camera(const __grid_constant__ DevScene S, PathState P, uint64_t g0, uint32_t n,
+                         uint32_t* q_active, uint32_t* active_count) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  init_path(S, P, i, g0 + i);
+  q_active[i] = i;
+  if (i == 0) *active_count = n;
+}
+
+// Shared wavefront of several jobs: slot i belongs to the segment whose
+// [start, start + count) holds it; the path is that job's index g0 + (i - start).
+__global__ void k_camera_multi(PathState P, const WaveSegment* segs, uint32_t nseg, uint32_t n, uint32_t* q_active,
+                               uint32_t* active_count) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t lo = 0, hi = nseg;
+  while (hi - lo > 1) {
+    uint32_t mid = (lo + hi) / 2;
+    if (segs[mid].start <= i) lo = mid;
+    else hi = mid;
+  }
+  const WaveSegment sg = segs[lo];
+  P.job[i] = sg.slot;
+  init_path(P.jobs[sg.slot], P, i, sg.g0 + (i - sg.start));
   q_active[i] = i;
   if (i == 0) *active_count = n;
 }
 
 // ------------------------------------------------------------------ trace
-template <bool BRUTE, bool COUNT>
-__global__ void __launch_bounds__(256) k_trace(const __grid_constant__ DevScene S, PathState P, QueueSet Q) {
+template <bool BRUTE, bool COUNT, bool MULTI>
+__global__ void __launch_bounds__(256) k_trace(const __grid_constant__ DevScene S0, PathState P, QueueSet Q) {
   const uint32_t n = *Q.in_count;
   TravCount tc;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     uint32_t p = Q.in[i];
+    const DevScene& S = MULTI ? P.jobs[P.job[p]] : S0;
     float4 o4 = P.ray_o[p], d4 = P.ray_d[p];
     HitRec h = trace_closest<BRUTE, COUNT>(S, f3(o4), f3(d4), 0.0f, WORLD_SIZE, &tc);
     P.hit[p] = make_float4(h.t, h.u, h.v, __uint_as_float(h.id));
@@ -339,10 +362,12 @@ __device__ __forceinline__ void fill_surface(const DevScene& S, float3 o, float3
 
 // ------------------------------------------------------------------ miss / emitter / invalid
 // pathtracer.rgen.glsl:70-115
-__global__ void __launch_bounds__(256) k_shade_logic(const __grid_constant__ DevScene S, PathState P, QueueSet Q) {
+template <bool MULTI>
+__global__ void __launch_bounds__(256) k_shade_logic(const __grid_constant__ DevScene S0, PathState P, QueueSet Q) {
   const uint32_t n = Q.counts[Q_LOGIC];
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     uint32_t p = Q.logic[i];
+    const DevScene& S = MULTI ? P.jobs[P.job[p]] : S0;
     float4 h = P.hit[p];
     uint32_t id = __float_as_uint(h.w);
     float4 r4 = P.rad[p];
@@ -475,14 +500,15 @@ struct Shader {
 // the visibility events, in the reference's order).
 constexpr uint32_t PEND_ENV = 1u, PEND_LIGHT = 2u, PEND_BSDF = 4u, PEND_STOP = 8u, PEND_RR = 16u;
 
-template <int MAT, bool MEDIUM, bool TRANSPARENT>
-__global__ void __launch_bounds__(256) k_shade(const __grid_constant__ DevScene S, PathState P, QueueSet Q) {
+template <int MAT, bool MEDIUM, bool TRANSPARENT, bool MULTI>
+__global__ void __launch_bounds__(256) k_shade(const __grid_constant__ DevScene S0, PathState P, QueueSet Q) {
   const int slot = MAT == PT_MATERIAL_DISNEY ? Q_DISNEY : Q_DIFFUSE;
   const uint32_t* qin = MAT == PT_MATERIAL_DISNEY ? Q.disney : Q.diffuse;
   const uint32_t n = Q.counts[slot];
   unsigned long long nshadow_total = 0;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     uint32_t p = qin[i];
+    const DevScene& S = MULTI ? P.jobs[P.job[p]] : S0;
     Shader<MAT> sh{S, P.rng[p], 0u, 0ull};
     float4 h = P.hit[p];
     float3 o = f3(P.ray_o[p]), d = f3(P.ray_d[p]);
@@ -676,11 +702,12 @@ __global__ void __launch_bounds__(256) k_shade(const __grid_constant__ DevScene 
 
 // ------------------------------------------------------------------ shadow rays
 // inc/lighting.glsl:116-149 and :203-238 (visibility + radiance += T * Ld)
-template <bool BRUTE>
-__global__ void __launch_bounds__(256) k_shadow(const __grid_constant__ DevScene S, PathState P, QueueSet Q) {
+template <bool BRUTE, bool MULTI>
+__global__ void __launch_bounds__(256) k_shadow(const __grid_constant__ DevScene S0, PathState P, QueueSet Q) {
   const uint32_t n = Q.counts[Q_SHADOW];
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     uint32_t p = Q.shadow[i];
+    const DevScene& S = MULTI ? P.jobs[P.job[p]] : S0;
     float4 so = P.sh_o[p];
     uint32_t pend = __float_as_uint(so.w);
     float3 o = f3(so);
@@ -716,7 +743,8 @@ __global__ void __launch_bounds__(256) k_shadow(const __grid_constant__ DevScene
 // Global path index g = frame * WH + pixel (frame counted from the last
 // reset); the wave holds g in [g0, g0 + n), its slot is g - g0.
 __global__ void k_accumulate(PathState P, uint64_t g0, uint32_t n, uint32_t WH, float4* accum, float4* albedo,
-                             float4* normal, float4* keep_rad, uint32_t* keep_hash, uint64_t keep_g0) {
+                             float4* normal, float4* keep_rad, uint32_t* keep_hash, uint64_t keep_g0,
+                             uint32_t wave_off) {
   uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
   if (pix >= WH) return;
   const uint64_t g1 = g0 + n;
@@ -724,7 +752,7 @@ __global__ void k_accumulate(PathState P, uint64_t g0, uint32_t n, uint32_t WH, 
   if (g >= g1) return;
   float4 a = accum[pix], b = albedo[pix], c = normal[pix];
   for (; g < g1; g += WH) {
-    uint32_t i = (uint32_t)(g - g0);
+    uint32_t i = wave_off + (uint32_t)(g - g0);
     float4 r = P.rad[i];
     float4 al = P.albedo[i];
     float4 nm = P.normal[i];
@@ -791,38 +819,58 @@ void launch_camera(const DevScene& S, const PathState& P, uint64_t g0, uint32_t 
 void launch_trace(const DevScene& S, const PathState& P, const QueueSet& Q, uint32_t max_items, bool count,
                   cudaStream_t st) {
   int g = grid_for(max_items);
-  if (count) k_trace<false, true><<<g, 256, 0, st>>>(S, P, Q);
-  else k_trace<false, false><<<g, 256, 0, st>>>(S, P, Q);
+  const bool multi = P.job != nullptr;
+  if (multi) {
+    if (count) k_trace<false, true, true><<<g, 256, 0, st>>>(S, P, Q);
+    else k_trace<false, false, true><<<g, 256, 0, st>>>(S, P, Q);
+  } else {
+    if (count) k_trace<false, true, false><<<g, 256, 0, st>>>(S, P, Q);
+    else k_trace<false, false, false><<<g, 256, 0, st>>>(S, P, Q);
+  }
+}
+
+template <bool MULTI>
+static void shade_all(const DevScene& S, const PathState& P, const QueueSet& Q, int g, bool med, bool tr,
+                      cudaStream_t st) {
+  k_shade_logic<MULTI><<<g, 256, 0, st>>>(S, P, Q);
+  if (med) {
+    if (tr) {
+      k_shade<PT_MATERIAL_DIFFUSE, true, true, MULTI><<<g, 256, 0, st>>>(S, P, Q);
+      k_shade<PT_MATERIAL_DISNEY, true, true, MULTI><<<g, 256, 0, st>>>(S, P, Q);
+    } else {
+      k_shade<PT_MATERIAL_DIFFUSE, true, false, MULTI><<<g, 256, 0, st>>>(S, P, Q);
+      k_shade<PT_MATERIAL_DISNEY, true, false, MULTI><<<g, 256, 0, st>>>(S, P, Q);
+    }
+  } else {
+    if (tr) {
+      k_shade<PT_MATERIAL_DIFFUSE, false, true, MULTI><<<g, 256, 0, st>>>(S, P, Q);
+      k_shade<PT_MATERIAL_DISNEY, false, true, MULTI><<<g, 256, 0, st>>>(S, P, Q);
+    } else {
+      k_shade<PT_MATERIAL_DIFFUSE, false, false, MULTI><<<g, 256, 0, st>>>(S, P, Q);
+      k_shade<PT_MATERIAL_DISNEY, false, false, MULTI><<<g, 256, 0, st>>>(S, P, Q);
+    }
+    k_shadow<false, MULTI><<<g, 256, 0, st>>>(S, P, Q);
+  }
 }
 
 void launch_shade(const DevScene& S, const PathState& P, const QueueSet& Q, uint32_t max_items, cudaStream_t st) {
   int g = grid_for(max_items);
-  k_shade_logic<<<g, 256, 0, st>>>(S, P, Q);
   const bool med = (S.features & PT_FEATURE_MEDIUM) != 0;
   const bool tr = (S.features & PT_FEATURE_TRANSPARENT) != 0;
-  if (med) {
-    if (tr) {
-      k_shade<PT_MATERIAL_DIFFUSE, true, true><<<g, 256, 0, st>>>(S, P, Q);
-      k_shade<PT_MATERIAL_DISNEY, true, true><<<g, 256, 0, st>>>(S, P, Q);
-    } else {
-      k_shade<PT_MATERIAL_DIFFUSE, true, false><<<g, 256, 0, st>>>(S, P, Q);
-      k_shade<PT_MATERIAL_DISNEY, true, false><<<g, 256, 0, st>>>(S, P, Q);
-    }
-  } else {
-    if (tr) {
-      k_shade<PT_MATERIAL_DIFFUSE, false, true><<<g, 256, 0, st>>>(S, P, Q);
-      k_shade<PT_MATERIAL_DISNEY, false, true><<<g, 256, 0, st>>>(S, P, Q);
-    } else {
-      k_shade<PT_MATERIAL_DIFFUSE, false, false><<<g, 256, 0, st>>>(S, P, Q);
-      k_shade<PT_MATERIAL_DISNEY, false, false><<<g, 256, 0, st>>>(S, P, Q);
-    }
-    k_shadow<false><<<g, 256, 0, st>>>(S, P, Q);
-  }
+  if (P.job) shade_all<true>(S, P, Q, g, med, tr, st);
+  else shade_all<false>(S, P, Q, g, med, tr, st);
+}
+
+void launch_camera_multi(const PathState& P, const WaveSegment* segs, uint32_t nseg, uint32_t n, uint32_t* q_active,
+                         uint32_t* active_count, cudaStream_t st) {
+  k_camera_multi<<<(n + 255) / 256, 256, 0, st>>>(P, segs, nseg, n, q_active, active_count);
 }
 
 void launch_accumulate(const PathState& P, uint64_t g0, uint32_t n, uint32_t WH, float4* accum, float4* albedo,
-                       float4* normal, float4* keep_rad, uint32_t* keep_hash, uint64_t keep_g0, cudaStream_t st) {
-  k_accumulate<<<(WH + 255) / 256, 256, 0, st>>>(P, g0, n, WH, accum, albedo, normal, keep_rad, keep_hash, keep_g0);
+                       float4* normal, float4* keep_rad, uint32_t* keep_hash, uint64_t keep_g0, cudaStream_t st,
+                       uint32_t wave_off) {
+  k_accumulate<<<(WH + 255) / 256, 256, 0, st>>>(P, g0, n, WH, accum, albedo, normal, keep_rad, keep_hash, keep_g0,
+                                                 wave_off);
 }
 
 void launch_finalize(const float4* accum, uchar4* final_img, uint32_t WH, float ev, int enable, int aces, int simple,

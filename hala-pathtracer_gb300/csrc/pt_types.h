@@ -103,6 +103,20 @@ struct PathState {
   float4* sh_c0;     // env contribution, (unused)
   float4* sh_c1;     // light contribution, pending hash events
   float4* sh_T;      // throughput at the NEE vertex
+  // shared wavefronts of several jobs (serving): per-path job slot and the
+  // device table of the jobs' scene records; null for a single-scene render
+  uint32_t* job;
+  const struct DevScene* jobs;
+};
+
+// One contiguous run of a job's paths inside a shared wavefront: wave slots
+// [start, start + count) hold the job's global path indices g0 .. g0 + count.
+struct WaveSegment {
+  uint32_t slot;
+  uint32_t start;
+  uint32_t count;
+  uint32_t pad;
+  uint64_t g0;
 };
 
 constexpr uint32_t ANS_BIT = 0x100u;        // any_non_specular_bounce

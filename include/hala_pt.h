@@ -311,6 +311,113 @@ pt_status pt_bvh_build_noalloc(const void* tri_v0, const void* tri_e1, const voi
                                void* tri_sorted_out, uint32_t* num_nodes_out, void* stream,
                                char* error_message, size_t error_capacity);
 
+/* ---- job server: continuous batching of render jobs ------------------------
+ * No counterpart in the reference, which renders one scene in one window
+ * (src/bin/hala-pathtracer.rs:226-295). A job is one render of one scene --
+ * what the reference does between set_scene and its last render() -- and the
+ * server runs many at once: a scheduler thread admits queued jobs while their
+ * estimated device memory fits the HBM budget and a job slot is free, keeps
+ * each admitted job's scene, BVH and accumulators on the device, and packs the
+ * paths of all admitted jobs with the same feature permutation into shared
+ * wavefronts. Jobs join and leave at wavefront boundaries. A job's images do
+ * not depend on which jobs it shared wavefronts with: they are bit-identical
+ * to a pt_renderer render of the same scene and configuration.
+ *
+ * Thread safety: every pt_server_* call may come from any host thread. */
+typedef struct pt_server pt_server;
+
+typedef struct pt_server_config {
+  uint64_t hbm_budget_bytes; /* device bytes for admitted jobs; 0 = 80% of free memory at create */
+  uint32_t max_jobs;         /* admitted (device-resident) jobs at most; 0 = 64 */
+  uint32_t wave_paths;       /* shared wavefront capacity in paths; 0 = 1 << 22 */
+  uint32_t quantum_paths;    /* paths a job gets per wavefront before the next job's turn; 0 = 1 << 18 */
+  uint32_t use_graphs;       /* 1 = replay each bounce as a CUDA graph */
+  uint64_t fail_admission_of_job; /* host-side fault injection: admission of this job id fails as if
+                                     the device were out of memory; 0 = off */
+} pt_server_config;
+
+/* One render job: the calls a reference host makes for one image. Host
+ * arrays are copied before pt_server_submit returns. */
+typedef struct pt_job_desc {
+  const pt_scene_desc* scene;   /* set_scene */
+  pt_tracer_config config;      /* HalaRenderer::new; wave_paths and keep_samples are ignored */
+  uint32_t frames;              /* render() calls = samples per pixel */
+  uint32_t camera_index;
+  const float* env_rgb;         /* set_envmap: RGB32F, env_width x env_height; NULL = sky */
+  uint32_t env_width;
+  uint32_t env_height;
+  float env_rotation_deg;
+  float ground_color[4];        /* set_ground_color */
+  float sky_color[4];           /* set_sky_color */
+  float env_intensity;          /* set_env_intensity */
+  float exposure_value;         /* set_exposure_value */
+} pt_job_desc;
+
+typedef enum pt_job_state {
+  PT_JOB_QUEUED = 0,     /* waiting for budget or a slot */
+  PT_JOB_RUNNING = 1,    /* admitted: resident on the device, sharing wavefronts */
+  PT_JOB_DONE = 2,       /* all frames accumulated and tonemapped; images readable */
+  PT_JOB_FAILED = 3,     /* see pt_job_info.status and .error */
+  PT_JOB_CANCELLED = 4
+} pt_job_state;
+
+typedef struct pt_job_info {
+  uint64_t id;
+  int32_t state;          /* pt_job_state */
+  int32_t status;         /* pt_status of a failed job */
+  uint64_t paths_total;   /* width * height * frames */
+  uint64_t paths_done;
+  uint64_t device_bytes;  /* admission estimate */
+  double submit_ms;       /* host clock, ms since the server was created */
+  double admit_ms;        /* admitted to the device (0 while queued) */
+  double done_ms;         /* reached a final state (0 before) */
+  char error[128];
+} pt_job_info;
+
+typedef struct pt_server_stats {
+  uint64_t jobs_submitted;
+  uint64_t jobs_done;
+  uint64_t jobs_failed;
+  uint64_t jobs_cancelled;
+  uint64_t jobs_rejected;      /* refused at submit (invalid, or larger than the whole budget) */
+  uint32_t jobs_queued;
+  uint32_t jobs_running;
+  uint64_t resident_bytes;     /* admission estimates of the admitted jobs */
+  uint64_t peak_resident_bytes;
+  uint64_t wavefronts;
+  uint64_t paths;
+  uint64_t closest_rays;
+  uint64_t shadow_rays;
+  uint64_t kernel_launches;
+  uint64_t graph_launches;
+  double busy_ms;              /* device time of all wavefronts (CUDA events) */
+  double uptime_ms;
+} pt_server_stats;
+
+pt_status pt_server_create(const pt_server_config* config, pt_server** out);
+/* Cancels what is still queued or running, waits for the scheduler, frees
+ * everything. */
+void pt_server_destroy(pt_server* s);
+const char* pt_server_last_error(const pt_server* s);
+/* Queues a job. PT_ERR_INVALID_ARG for an invalid scene or configuration,
+ * PT_ERR_OOM when the job alone exceeds the whole budget; neither is queued. */
+pt_status pt_server_submit(pt_server* s, const pt_job_desc* job, uint64_t* job_id);
+pt_status pt_server_poll(pt_server* s, uint64_t job_id, pt_job_info* info);
+/* Waits until the job reaches a final state: PT_OK, or PT_ERR_TIMEOUT after
+ * timeout_ms (0 = no limit). */
+pt_status pt_server_wait(pt_server* s, uint64_t job_id, uint32_t timeout_ms);
+/* Images of a PT_JOB_DONE job (accum, albedo, normal, final). */
+pt_status pt_server_read_image(pt_server* s, uint64_t job_id, pt_image which, void* host, size_t bytes);
+/* A queued job is cancelled at once, a running one at the next wavefront
+ * boundary. */
+pt_status pt_server_cancel(pt_server* s, uint64_t job_id);
+/* Frees a finished job's device memory and forgets it (a job that is not
+ * finished is cancelled first). */
+pt_status pt_server_release(pt_server* s, uint64_t job_id);
+/* 1 = stop forming wavefronts (queued jobs are still admitted), 0 = go on. */
+pt_status pt_server_pause(pt_server* s, int32_t paused);
+pt_status pt_server_get_stats(pt_server* s, pt_server_stats* out);
+
 /* ---- helpers ------------------------------------------------------------- */
 
 /* Fills ax/ay from roughness/anisotropic the way the shaders expect them
