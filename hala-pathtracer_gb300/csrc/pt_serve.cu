@@ -504,7 +504,7 @@ pt_status pt_server_create(const pt_server_config* cfg, pt_server** out) {
   if (cfg) s->cfg = *cfg;
   cudaGetDevice(&s->device);
   if (s->cfg.max_jobs == 0) s->cfg.max_jobs = 64;
-  if (s->cfg.wave_paths == 0) s->cfg.wave_paths = 1u << 22;
+  if (s->cfg.wave_paths == 0) s->cfg.wave_paths = 1u << 25;
   if (s->cfg.quantum_paths == 0) s->cfg.quantum_paths = 1u << 18;
   if (s->cfg.hbm_budget_bytes == 0) {
     size_t fr = 0, tot = 0;

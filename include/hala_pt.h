@@ -329,7 +329,7 @@ typedef struct pt_server pt_server;
 typedef struct pt_server_config {
   uint64_t hbm_budget_bytes; /* device bytes for admitted jobs; 0 = 80% of free memory at create */
   uint32_t max_jobs;         /* admitted (device-resident) jobs at most; 0 = 64 */
-  uint32_t wave_paths;       /* shared wavefront capacity in paths; 0 = 1 << 22 */
+  uint32_t wave_paths;       /* shared wavefront capacity in paths; 0 = 1 << 25 */
   uint32_t quantum_paths;    /* paths a job gets per wavefront before the next job's turn; 0 = 1 << 18 */
   uint32_t use_graphs;       /* 1 = replay each bounce as a CUDA graph */
   uint64_t fail_admission_of_job; /* host-side fault injection: admission of this job id fails as if
