@@ -155,6 +155,12 @@ class Renderer:
         self._check(self._lib.pt_renderer_get_stats(self._h, C.byref(s)))
         return s
 
+    def set_radiance_cache(self, enable=True, **options):
+        """Attaches a new online radiance cache (options: pt_cache_config
+        fields) or, with enable=False, detaches it (plain unbiased tracer)."""
+        cfg = _cache_config(**options) if enable else None
+        self._check(self._lib.pt_renderer_set_radiance_cache(self._h, C.byref(cfg) if cfg is not None else None))
+
     def set_profiling(self, flags):
         """abi.PROFILE_TRACE_TIMING | abi.PROFILE_COUNT, or 0."""
         self._check(self._lib.pt_renderer_set_profiling(self._h, int(flags)))
@@ -188,3 +194,13 @@ def renderer_for(scene, **cfg_over):
     r.set_exposure_value(scene.exposure_value)
     r.commit()
     return r
+
+
+def _cache_config(**kw):
+    cfg = abi.CacheConfig()
+    load_library().pt_cache_config_default(C.byref(cfg))
+    for k, v in kw.items():
+        if not hasattr(cfg, k):
+            raise TypeError(f"unknown radiance-cache option {k}")
+        setattr(cfg, k, v)
+    return cfg

@@ -104,7 +104,16 @@ class Stats(C.Structure):
                 ("triangles", C.c_uint64), ("features", C.c_uint32),
                 ("max_bounces_seen", C.c_uint32), ("trace_launches", C.c_uint64),
                 ("trav_nodes", C.c_uint64), ("trav_tris", C.c_uint64),
-                ("kernel_launches", C.c_uint64)]
+                ("kernel_launches", C.c_uint64), ("cache_queries", C.c_uint64),
+                ("cache_train_samples", C.c_uint64), ("cache_train_steps", C.c_uint64),
+                ("cache_loss", C.c_double)]
+
+
+class CacheConfig(C.Structure):
+    _fields_ = [("query_depth", C.c_uint32), ("train_shift", C.c_uint32), ("batch_size", C.c_uint32),
+                ("log2_table_size", C.c_uint32), ("learning_rate", C.c_float),
+                ("min_resolution", C.c_uint32), ("max_resolution", C.c_uint32), ("seed", C.c_uint32),
+                ("warmup_frames", C.c_uint32)]
 
 
 class ServerConfig(C.Structure):
@@ -202,6 +211,20 @@ RENDERER_SIGNATURES = {
     "pt_server_release": (C.c_int, [C.c_void_p, C.c_uint64]),
     "pt_server_pause": (C.c_int, [C.c_void_p, C.c_int32]),
     "pt_server_get_stats": (C.c_int, [C.c_void_p, C.POINTER(ServerStats)]),
+    "pt_cache_config_default": (None, [C.POINTER(CacheConfig)]),
+    "pt_cache_create": (C.c_int, [C.POINTER(CacheConfig), C.POINTER(C.c_void_p)]),
+    "pt_cache_destroy": (None, [C.c_void_p]),
+    "pt_cache_last_error": (C.c_char_p, [C.c_void_p]),
+    "pt_cache_set_bounds": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "pt_cache_num_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "pt_cache_get_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "pt_cache_set_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "pt_cache_infer": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "pt_cache_gradients": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
+                                     C.c_void_p, C.POINTER(C.c_float)]),
+    "pt_cache_train": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                 C.POINTER(C.c_float)]),
+    "pt_renderer_set_radiance_cache": (C.c_int, [C.c_void_p, C.POINTER(CacheConfig)]),
     "pt_material_preprocess": (None, [C.POINTER(Material)]),
     "pt_material_default": (None, [C.POINTER(Material)]),
     "pt_abi_version": (C.c_uint32, []),

@@ -13,6 +13,7 @@
 #include <string>
 #include <vector>
 
+#include "pt_cache.h"
 #include "pt_impl.h"
 
 namespace hpt {
@@ -336,6 +337,67 @@ bool write_pfm(const char* path, const float4* px, uint32_t w, uint32_t h) {
   return std::fclose(f) == 0;
 }
 
+// Creates the renderer's cache on first use (bounds from the BVH root) and
+// sizes its per-path buffers for wavefronts of `cap` paths.
+pt_status cache_prepare(pt_renderer* r, uint32_t cap) {
+  if (r->features & PT_FEATURE_MEDIUM)
+    return fail(r, PT_ERR_UNSUPPORTED, "the radiance cache does not support participating media");
+  if (!r->cache) {
+    pt_status cs = pt_cache_create(&r->cache_cfg, &r->cache);
+    if (cs != PT_OK) return fail(r, cs, "radiance cache creation failed");
+    float lo[3] = {-1, -1, -1}, hi[3] = {1, 1, 1};
+    if (r->nnodes > 0) {
+      float4 root[4];
+      CK(r, cudaMemcpy(root, r->nodes.p, sizeof(root), cudaMemcpyDeviceToHost));
+      float b[6] = {std::fmin(root[0].x, root[1].x), std::fmax(root[0].y, root[1].y),
+                    std::fmin(root[0].z, root[1].z), std::fmax(root[0].w, root[1].w),
+                    std::fmin(root[2].x, root[2].z), std::fmax(root[2].y, root[2].w)};
+      for (int i = 0; i < 3; ++i) {
+        float l = b[2 * i], h = b[2 * i + 1];
+        if (!(h > l)) {
+          l -= 1.0f;
+          h += 1.0f;
+        }
+        float pad = 1e-3f * (h - l);
+        lo[i] = l - pad;
+        hi[i] = h + pad;
+      }
+    }
+    pt_cache_set_bounds(r->cache, lo, hi);
+  }
+  if (r->c_cap < cap) {
+    CK(r, r->c_rec.ensure(4 * (size_t)cap));
+    CK(r, r->c_T.ensure(cap));
+    CK(r, r->t_rec.ensure(4 * (size_t)cap));
+    CK(r, r->t_T.ensure(cap));
+    CK(r, r->t_R.ensure(cap));
+    CK(r, r->c_tgt.ensure(cap));
+    CK(r, r->c_queue.ensure(cap));
+    CK(r, r->c_train.ensure(cap));
+    CK(r, r->c_counts.ensure(2));
+    r->c_cap = cap;
+  }
+  PathState& P = r->W.P;
+  P.c_rec = r->c_rec.p;
+  P.c_T = r->c_T.p;
+  P.c_queue = r->c_queue.p;
+  P.c_counts = r->c_counts.p;
+  P.c_train = r->c_train.p;
+  P.t_rec = r->t_rec.p;
+  P.t_T = r->t_T.p;
+  P.t_R = r->t_R.p;
+  P.c_depth = r->cache_cfg.query_depth;
+  P.c_shift = r->cache_cfg.train_shift;
+  P.c_mode = 2;
+  return PT_OK;
+}
+
+void cache_detach(pt_renderer* r) {
+  PathState& P = r->W.P;
+  P.c_rec = P.c_T = P.t_rec = P.t_T = P.t_R = nullptr;
+  P.c_queue = P.c_counts = P.c_train = nullptr;
+}
+
 }  // namespace
 
 extern "C" {
@@ -411,6 +473,7 @@ void pt_renderer_destroy(pt_renderer* r) {
   if (r->ev1) cudaEventDestroy(r->ev1);
   if (r->pinned) cudaFreeHost(r->pinned);
   for (cudaEvent_t e : r->tev) cudaEventDestroy(e);
+  if (r->cache) pt_cache_destroy(r->cache);
   cudaStream_t s = r->stream;
   delete r;
   if (s) cudaStreamDestroy(s);
@@ -625,18 +688,57 @@ pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) {
   BounceLoop L;
   L.profiling = r->profiling;
   L.tev = &r->tev;
-  for (uint64_t off = 0; off < total; off += cap) {
+  const bool use_cache = r->cache_on;
+  if (use_cache) {
+    pt_status cs = cache_prepare(r, cap);
+    if (cs != PT_OK) return cs;
+  }
+  uint64_t c_queries = 0, c_samples = 0, c_steps = 0;
+  for (uint64_t off = 0; off < total;) {
     uint32_t n = (uint32_t)std::min<uint64_t>(cap, total - off);
+    PathState P = r->W.P;
+    if (use_cache) {
+      // warm-up: the first frames after the cache is attached train only
+      const uint64_t warm = (uint64_t)r->cache_cfg.warmup_frames * WH;
+      P.c_mode = r->cache_paths_seen < warm ? 1u : 2u;
+      if (P.c_mode == 1) n = (uint32_t)std::min<uint64_t>(n, warm - r->cache_paths_seen);
+      CK(r, cudaMemsetAsync(r->c_counts.p, 0, 2 * sizeof(uint32_t), st));
+    }
     uint64_t g0 = g_start + off;
-    launch_camera(r->view, r->W.P, g0, n, r->W.q_a.p, r->W.counters.p + Q_COUNT + Q_NEXT, st);
-    CK(r, run_bounces(r->view, r->W, n, r->cfg.max_depth, L, r->pinned, st));
+    launch_camera(r->view, P, g0, n, r->W.q_a.p, r->W.counters.p + Q_COUNT + Q_NEXT, st);
+    {
+      WaveBuffers& W = r->W;
+      PathState keep = W.P;
+      W.P = P;
+      cudaError_t be = run_bounces(r->view, W, n, r->cfg.max_depth, L, r->pinned, st);
+      W.P = keep;
+      CK(r, be);
+    }
     if (L.timed_out) return fail(r, PT_ERR_TIMEOUT, "paths still alive after the bounce cap");
     max_bounces = std::max(max_bounces, L.bounces);
     launches += 2 + per_bounce * L.bounces;  // camera + accumulate + bounces
-    launch_accumulate(r->W.P, g0, n, WH, r->accum.p, r->albedo.p, r->normal.p,
+    if (use_cache && P.c_mode == 2) {
+      launch_cache_infer(cache_view(r->cache), P.c_rec, P.c_queue, P.c_counts, n, P.rad, P.c_T, st);
+      ++launches;
+    }
+    launch_accumulate(P, g0, n, WH, r->accum.p, r->albedo.p, r->normal.p,
                       r->cfg.keep_samples ? r->keep_rad.p : nullptr, r->cfg.keep_samples ? r->keep_hash.p : nullptr,
                       g_start, st);
     CK(r, cudaGetLastError());
+    if (use_cache) {
+      launch_cache_targets(P, n, r->c_tgt.p, st);
+      CK(r, cudaMemcpyAsync(r->pinned + 4, r->c_counts.p, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+      CK(r, cudaStreamSynchronize(st));
+      const uint32_t nq = r->pinned[4], ns = r->pinned[5];
+      uint32_t steps = 0;
+      CK(r, cache_train_device(r->cache, r->t_rec.p, r->c_tgt.p, ns, st, &steps));
+      c_queries += P.c_mode == 2 ? nq : 0;
+      c_samples += ns;
+      c_steps += steps;
+      launches += 1 + 4ull * steps;  // targets + per step: forward/backward, dW, two Adam kernels
+      r->cache_paths_seen += n;
+    }
+    off += n;
   }
   const size_t ntimed = L.ntimed;
   launch_finalize(r->accum.p, r->final_img.p, WH, r->exposure, r->cfg.enable_tonemap, r->cfg.enable_aces,
@@ -659,6 +761,14 @@ pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) {
   r->stats.trav_tris = rays[3];
   r->stats.trace_launches = ntimed;
   r->stats.kernel_launches = launches + 1;  // + finalize
+  r->stats.cache_queries = c_queries;
+  r->stats.cache_train_samples = c_samples;
+  r->stats.cache_train_steps = c_steps;
+  if (use_cache) {
+    float lossv = 0.0f;
+    cache_last_loss(r->cache, &lossv);
+    r->stats.cache_loss = lossv;
+  }
   double tms = 0.0;
   for (size_t k = 0; k < ntimed; ++k) {
     float e = 0.0f;
@@ -666,6 +776,37 @@ pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) {
     tms += e;
   }
   r->stats.trace_ms = tms;
+  return PT_OK;
+}
+
+pt_status pt_renderer_set_radiance_cache(pt_renderer* r, const pt_cache_config* cfg) {
+  if (!r) return PT_ERR_INVALID_ARG;
+  CK(r, cudaStreamSynchronize(r->stream));
+  if (r->cache) pt_cache_destroy(r->cache);
+  r->cache = nullptr;
+  r->cache_paths_seen = 0;
+  cache_detach(r);
+  if (!cfg) {
+    r->cache_on = false;
+    return PT_OK;
+  }
+  pt_cache_config c;
+  pt_cache_config_default(&c);
+  c.query_depth = cfg->query_depth;
+  c.train_shift = cfg->train_shift;
+  c.warmup_frames = cfg->warmup_frames;
+  if (cfg->batch_size) c.batch_size = cfg->batch_size;
+  if (cfg->log2_table_size) c.log2_table_size = cfg->log2_table_size;
+  if (cfg->learning_rate > 0.0f) c.learning_rate = cfg->learning_rate;
+  if (cfg->min_resolution) c.min_resolution = cfg->min_resolution;
+  if (cfg->max_resolution) c.max_resolution = cfg->max_resolution;
+  c.seed = cfg->seed;
+  if (c.query_depth == 0) return fail(r, PT_ERR_INVALID_ARG, "query_depth must be at least 1");
+  if (c.train_shift > 16) return fail(r, PT_ERR_INVALID_ARG, "train_shift must be at most 16");
+  if (r->committed && (r->features & PT_FEATURE_MEDIUM))
+    return fail(r, PT_ERR_UNSUPPORTED, "the radiance cache does not support participating media");
+  r->cache_cfg = c;
+  r->cache_on = true;
   return PT_OK;
 }
 

@@ -121,6 +121,15 @@ struct pt_renderer {
   pt_stats stats{};
   uint32_t profiling = 0;
   std::vector<cudaEvent_t> tev;  // start/stop pairs around closest-hit launches
+
+  // radiance cache (pt_renderer_set_radiance_cache)
+  bool cache_on = false;
+  pt_cache_config cache_cfg{};
+  pt_cache* cache = nullptr;
+  uint64_t cache_paths_seen = 0;  // paths rendered since the cache was attached
+  uint32_t c_cap = 0;
+  hpt::Buf<float4> c_rec, c_T, t_rec, t_T, t_R, c_tgt;
+  hpt::Buf<uint32_t> c_queue, c_train, c_counts;
 };
 
 namespace hpt {

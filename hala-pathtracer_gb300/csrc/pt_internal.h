@@ -34,6 +34,7 @@ void launch_camera_multi(const PathState& P, const WaveSegment* segs, uint32_t n
 void launch_accumulate(const PathState& P, uint64_t g0, uint32_t n, uint32_t WH, float4* accum, float4* albedo,
                        float4* normal, float4* keep_rad, uint32_t* keep_hash, uint64_t keep_g0, cudaStream_t st,
                        uint32_t wave_off = 0);
+void launch_cache_targets(const PathState& P, uint32_t n, float4* tgt, cudaStream_t st);
 void launch_finalize(const float4* accum, uchar4* final_img, uint32_t WH, float ev, int enable, int aces, int simple,
                      cudaStream_t st);
 void launch_trace_rays(const DevScene& S, const float4* rays, uint32_t n, int any_hit, int brute, uint4* hits,

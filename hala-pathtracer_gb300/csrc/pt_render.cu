@@ -101,6 +101,7 @@ __device__ __forceinline__ void init_path(const DevScene& S, const PathState& P,
     P.med0[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     P.med1[i] = make_float2(1.0f, __uint_as_float(PT_MEDIUM_NONE));
   }
+  if (P.c_train) P.c_train[i] = 0xFFFFFFFFu;
 }
 
 __global__ void k_camera(const __grid_constant__ DevScene S, PathState P, uint64_t g0, uint32_t n,
@@ -500,7 +501,19 @@ struct Shader {
 // the visibility events, in the reference's order).
 constexpr uint32_t PEND_ENV = 1u, PEND_LIGHT = 2u, PEND_BSDF = 4u, PEND_STOP = 8u, PEND_RR = 16u;
 
-template <int MAT, bool MEDIUM, bool TRANSPARENT, bool MULTI>
+// Warp-aggregated append that returns the slot index (or ~0u when !pred).
+__device__ __forceinline__ uint32_t append_index(uint32_t* counter, bool pred) {
+  unsigned active = __activemask();
+  unsigned m = __ballot_sync(active, pred);
+  if (m == 0) return 0xFFFFFFFFu;
+  int leader = __ffs(m) - 1;
+  uint32_t base = 0;
+  if ((int)lane_id() == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
+  base = __shfl_sync(active, base, leader);
+  return pred ? base + __popc(m & ((1u << lane_id()) - 1u)) : 0xFFFFFFFFu;
+}
+
+template <int MAT, bool MEDIUM, bool TRANSPARENT, bool MULTI, bool CACHE = false>
 __global__ void __launch_bounds__(256) k_shade(const __grid_constant__ DevScene S0, PathState P, QueueSet Q) {
   const int slot = MAT == PT_MATERIAL_DISNEY ? Q_DISNEY : Q_DIFFUSE;
   const uint32_t* qin = MAT == PT_MATERIAL_DISNEY ? Q.disney : Q.diffuse;
@@ -536,6 +549,35 @@ __global__ void __launch_bounds__(256) k_shade(const __grid_constant__ DevScene 
     const pt_material& mat = S.mats[st.mat];
     st.fr.eta = dot(d, st.normal) < 0.0f ? (1.0f / mat.ior) : mat.ior;
     st.fr.depth = depth;
+    if (CACHE && depth == P.c_depth) {
+      // radiance-cache vertex: the path either ends here with the cache's
+      // estimate (added after the bounce loop) or continues as a training path
+      const float4 rec0 = make_float4(st.fhp.x, st.fhp.y, st.fhp.z, -d.x);
+      const float4 rec1 = make_float4(-d.y, -d.z, st.ffnormal.x, st.ffnormal.y);
+      const float4 rec2 = make_float4(st.ffnormal.z, mat.base_color[0], mat.base_color[1], mat.base_color[2]);
+      const float4 rec3 = make_float4(mat.roughness, mat.metallic, mat.specular_transmission, 0.0f);
+      const bool train = P.c_mode == 1 || P.c_shift == 0 || ((p * 2654435761u) >> (32u - P.c_shift)) == 0u;
+      if (!train) {
+        P.c_rec[4 * (size_t)p] = rec0;
+        P.c_rec[4 * (size_t)p + 1] = rec1;
+        P.c_rec[4 * (size_t)p + 2] = rec2;
+        P.c_rec[4 * (size_t)p + 3] = rec3;
+        P.c_T[p] = make_float4(T.x, T.y, T.z, 0.0f);
+        queue_push(P.c_queue, &P.c_counts[0], p, true);
+        continue;
+      }
+      const bool fresh = P.c_train[p] == 0xFFFFFFFFu;
+      uint32_t k = append_index(&P.c_counts[1], fresh);
+      if (fresh) {
+        P.t_rec[4 * (size_t)k] = rec0;
+        P.t_rec[4 * (size_t)k + 1] = rec1;
+        P.t_rec[4 * (size_t)k + 2] = rec2;
+        P.t_rec[4 * (size_t)k + 3] = rec3;
+        P.t_T[k] = make_float4(T.x, T.y, T.z, 0.0f);
+        P.t_R[k] = make_float4(rad.x, rad.y, rad.z, 0.0f);
+        P.c_train[p] = k;
+      }
+    }
     if (depth == 0) {
       P.albedo[p] = make_float4(mat.base_color[0], mat.base_color[1], mat.base_color[2], 0.0f);
       P.normal[p] = make_float4(st.normal.x, st.normal.y, st.normal.z, 0.0f);
@@ -778,6 +820,19 @@ __global__ void k_accumulate(PathState P, uint64_t g0, uint32_t n, uint32_t WH, 
   normal[pix] = c;
 }
 
+// Training targets of the radiance cache: what the unbiased path gathered
+// from the cache vertex on, divided by the throughput arriving there.
+__global__ void k_cache_targets(PathState P, uint32_t n, float4* tgt) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t k = P.c_train[i];
+  if (k == 0xFFFFFFFFu) return;
+  float4 r = P.rad[i], R = P.t_R[k], T = P.t_T[k];
+  float3 y = make_float3(T.x > 0.0f ? (r.x - R.x) / T.x : 0.0f, T.y > 0.0f ? (r.y - R.y) / T.y : 0.0f,
+                         T.z > 0.0f ? (r.z - R.z) / T.z : 0.0f);
+  tgt[k] = make_float4(fmaxf(y.x, 0.0f), fmaxf(y.y, 0.0f), fmaxf(y.z, 0.0f), 0.0f);
+}
+
 // pathtracer.rgen.glsl:280-304
 __global__ void k_finalize(const float4* accum, uchar4* final_img, uint32_t WH, float ev, int enable, int aces,
                            int simple) {
@@ -857,8 +912,24 @@ void launch_shade(const DevScene& S, const PathState& P, const QueueSet& Q, uint
   int g = grid_for(max_items);
   const bool med = (S.features & PT_FEATURE_MEDIUM) != 0;
   const bool tr = (S.features & PT_FEATURE_TRANSPARENT) != 0;
+  if (P.c_rec && !P.job && !med) {
+    k_shade_logic<false><<<g, 256, 0, st>>>(S, P, Q);
+    if (tr) {
+      k_shade<PT_MATERIAL_DIFFUSE, false, true, false, true><<<g, 256, 0, st>>>(S, P, Q);
+      k_shade<PT_MATERIAL_DISNEY, false, true, false, true><<<g, 256, 0, st>>>(S, P, Q);
+    } else {
+      k_shade<PT_MATERIAL_DIFFUSE, false, false, false, true><<<g, 256, 0, st>>>(S, P, Q);
+      k_shade<PT_MATERIAL_DISNEY, false, false, false, true><<<g, 256, 0, st>>>(S, P, Q);
+    }
+    k_shadow<false, false><<<g, 256, 0, st>>>(S, P, Q);
+    return;
+  }
   if (P.job) shade_all<true>(S, P, Q, g, med, tr, st);
   else shade_all<false>(S, P, Q, g, med, tr, st);
+}
+
+void launch_cache_targets(const PathState& P, uint32_t n, float4* tgt, cudaStream_t st) {
+  k_cache_targets<<<(n + 255) / 256, 256, 0, st>>>(P, n, tgt);
 }
 
 void launch_camera_multi(const PathState& P, const WaveSegment* segs, uint32_t nseg, uint32_t n, uint32_t* q_active,

@@ -107,6 +107,18 @@ struct PathState {
   // device table of the jobs' scene records; null for a single-scene render
   uint32_t* job;
   const struct DevScene* jobs;
+  // radiance cache (all null when no cache is attached)
+  float4* c_rec;       // query record of a path that ends in the cache (4 float4 per slot)
+  float4* c_T;         // throughput arriving at the query vertex
+  uint32_t* c_queue;   // slots waiting for a cache query
+  uint32_t* c_counts;  // [0] queued queries, [1] training samples
+  uint32_t* c_train;   // training-sample index of the slot, ~0u = none
+  float4* t_rec;       // training samples: record (4 float4 each),
+  float4* t_T;         //   throughput arriving at the vertex,
+  float4* t_R;         //   radiance gathered before the vertex
+  uint32_t c_depth;    // vertex index of the query
+  uint32_t c_mode;     // 1 = every path trains (warm-up), 2 = query, 1 in 2^c_shift trains
+  uint32_t c_shift;
 };
 
 // One contiguous run of a job's paths inside a shared wavefront: wave slots

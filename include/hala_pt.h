@@ -206,6 +206,10 @@ typedef struct pt_stats {
   uint64_t trav_nodes;       /* BVH nodes visited by closest-hit rays (PT_PROFILE_COUNT) */
   uint64_t trav_tris;        /* triangle tests of closest-hit rays (PT_PROFILE_COUNT) */
   uint64_t kernel_launches;  /* kernels launched by the last render call */
+  uint64_t cache_queries;        /* paths ended in the radiance cache, last render call */
+  uint64_t cache_train_samples;  /* training samples gathered, last render call */
+  uint64_t cache_train_steps;    /* optimiser steps, last render call */
+  double cache_loss;             /* loss of the last training batch */
 } pt_stats;
 
 /* Profiling switches for pt_renderer_set_profiling. */
@@ -417,6 +421,63 @@ pt_status pt_server_release(pt_server* s, uint64_t job_id);
 /* 1 = stop forming wavefronts (queued jobs are still admitted), 0 = go on. */
 pt_status pt_server_pause(pt_server* s, int32_t paused);
 pt_status pt_server_get_stats(pt_server* s, pt_server_stats* out);
+
+/* ---- radiance cache --------------------------------------------------------
+ * No counterpart in the reference (its integrator is the plain unbiased path
+ * tracer of pathtracer.rgen.glsl). An online-trained neural radiance cache:
+ * a multiresolution hash-grid encoding of the query position (16 levels,
+ * 2^log2_table_size fp16 entries of 2 features per level) plus direction,
+ * normal and material inputs, feeding an MLP with 5 hidden layers of 64 ReLU
+ * units (BF16 weights, FP32 accumulation), trained with Adam on the relative
+ * L2 loss. With a cache attached to a renderer, paths end at vertex
+ * `query_depth` and take the cache's estimate of the radiance leaving that
+ * vertex; 1 in 2^train_shift paths continue unbiased and become training
+ * samples. Without a cache the renderer is the plain tracer.
+ *
+ * Query record (16 floats): position xyz, outgoing direction xyz (towards
+ * the previous vertex), shading normal xyz, base colour rgb, roughness,
+ * metallic, specular transmission, 0. */
+typedef struct pt_cache pt_cache;
+
+typedef struct pt_cache_config {
+  uint32_t query_depth;     /* vertex index at which paths end in the cache (1 = first bounce) */
+  uint32_t train_shift;     /* 1 in 2^train_shift paths trains the cache (4 = 1/16) */
+  uint32_t batch_size;      /* training batch in samples (multiple of 16) */
+  uint32_t log2_table_size; /* hash-table entries per level = 2^log2_table_size */
+  float learning_rate;      /* Adam learning rate */
+  uint32_t min_resolution;  /* coarsest grid level */
+  uint32_t max_resolution;  /* finest grid level */
+  uint32_t seed;            /* weight initialisation */
+  uint32_t warmup_frames;   /* frames traced with every path training before the first query */
+} pt_cache_config;
+
+/* query_depth 1, 1/16 training paths, batch 65536, 2^19 entries, lr 1e-2,
+ * resolutions 16..2048, seed 1, one warm-up frame. */
+void pt_cache_config_default(pt_cache_config* config);
+pt_status pt_cache_create(const pt_cache_config* config, pt_cache** out);
+void pt_cache_destroy(pt_cache* cache);
+const char* pt_cache_last_error(const pt_cache* cache);
+/* Scene box mapped to the unit cube of the encoding. */
+pt_status pt_cache_set_bounds(pt_cache* cache, const float lo[3], const float hi[3]);
+/* Parameter counts: MLP weights (layer by layer, [in][out] row-major) and
+ * hash-table floats ([level][entry][feature]). */
+pt_status pt_cache_num_params(const pt_cache* cache, uint64_t* mlp, uint64_t* grid);
+/* FP32 master parameters (either pointer may be NULL). */
+pt_status pt_cache_get_params(pt_cache* cache, float* mlp, float* grid);
+pt_status pt_cache_set_params(pt_cache* cache, const float* mlp, const float* grid);
+/* Predicted RGB (3 floats per record) for n host records. */
+pt_status pt_cache_infer(pt_cache* cache, const float* records, uint32_t n, float* out_rgb);
+/* Loss and gradients of one batch without updating anything (gradient check). */
+pt_status pt_cache_gradients(pt_cache* cache, const float* records, const float* targets_rgb, uint32_t n,
+                             float* mlp_grad, float* grid_grad, float* loss);
+/* `steps` passes of Adam over the n samples in batches of batch_size; the
+ * loss of the last batch goes to *last_loss. */
+pt_status pt_cache_train(pt_cache* cache, const float* records, const float* targets_rgb, uint32_t n,
+                         uint32_t steps, float* last_loss);
+/* Attaches a new cache to the renderer (NULL detaches it and renders
+ * unbiased again). The renderer owns the cache; scenes with participating
+ * media are refused (PT_ERR_UNSUPPORTED). */
+pt_status pt_renderer_set_radiance_cache(pt_renderer* r, const pt_cache_config* config);
 
 /* ---- helpers ------------------------------------------------------------- */
 
