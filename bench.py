@@ -156,6 +156,72 @@ def run_reference(args, scene, workload):
     return 0
 
 
+def cache_curves(pt, scene, ref, chunks, cache_options=None):
+    """Progressive render; after each chunk: (spp, device ms so far, RMSE
+    against `ref`, rays per path so far)."""
+    import numpy as np
+    r = pt.renderer_for(scene)
+    if cache_options is not None:
+        r.set_radiance_cache(**cache_options)
+    out, t, done, rays = [], 0.0, 0, 0
+    for c in chunks:
+        r.render(c)
+        st = r.stats()
+        t += st.render_ms
+        done += c
+        rays += st.closest_rays + st.shadow_rays
+        err = float(np.sqrt(((r.image(0)[..., :3].astype(np.float64) - ref) ** 2).mean()))
+        out.append((done, t, err, rays / (done * scene.width * scene.height)))
+    r.close()
+    return out
+
+
+def time_to_error(curve, target):
+    """Device time at which a curve first reaches `target` RMSE (log-log
+    interpolation between checkpoints), or None."""
+    prev = None
+    for spp, t, e, _ in curve:
+        if e <= target:
+            if prev is None:
+                return t
+            (t0, e0), (t1, e1) = prev, (t, e)
+            if e0 <= e1:
+                return t1
+            f = (math.log(e0) - math.log(target)) / (math.log(e0) - math.log(e1))
+            return math.exp(math.log(t0) + f * (math.log(t1) - math.log(t0)))
+        prev = (t, e)
+    return None
+
+
+def radiance_cache_leg(pt, target_spp=256):
+    """RMSE against the 4096-spp FP64 oracle image of the 128 x 128 Cornell
+    box (tests/golden/cornell128_4096spp_fp64.npz) versus device time, for
+    the plain tracer and with the online radiance cache."""
+    import numpy as np
+    scenes = importlib.import_module("hala-pathtracer_gb300.scenes")
+    ref = np.load(os.path.join(ROOT, "tests", "golden", "cornell128_4096spp_fp64.npz"))["radiance"].astype(np.float64)
+    s = scenes.cornell(128, 128, 1024, max_depth=8, rr_depth=0, seed=1)
+    chunks = [1, 1, 2, 4, 8, 16, 32, 64, 128, 256, 512]
+    warm = pt.renderer_for(s)
+    warm.render(2)
+    warm.set_radiance_cache()
+    warm.render(4)
+    warm.close()
+    plain = cache_curves(pt, s, ref, chunks)
+    cached = cache_curves(pt, s, ref, chunks, {})
+    target = next(e for spp, t, e, _ in plain if spp == target_spp)
+    t_plain = next(t for spp, t, e, _ in plain if spp == target_spp)
+    t_cache = time_to_error(cached, target)
+    return {
+        "scene": "cornell 128x128, depth 8, no RR", "reference": "oracle 4096 spp FP64",
+        "target_rmse": target, "plain_ms_to_target": t_plain, "cache_ms_to_target": t_cache,
+        "time_ratio": (t_cache / t_plain) if t_cache else None,
+        "plain_rmse_1024spp": plain[-1][2], "cache_rmse_1024spp": cached[-1][2],
+        "plain_rays_per_path": plain[-1][3], "cache_rays_per_path": cached[-1][3],
+        "plain_ms_1024spp": plain[-1][1], "cache_ms_1024spp": cached[-1][1],
+    }
+
+
 def serving_leg(n_jobs=256, rate=20.0, seed=0):
     """The serving mix: `n_jobs` render jobs with Poisson arrivals at `rate`
     jobs/s, scenes drawn from the four workloads with seed-perturbed
@@ -194,6 +260,7 @@ def main():
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving mix")
+    ap.add_argument("--no-cache", action="store_true", help="skip the radiance-cache comparison")
     ap.add_argument("--serving-jobs", type=int, default=256)
     args = ap.parse_args()
     if args.warmup < 3:
@@ -323,6 +390,11 @@ def main():
         except Exception as e:  # the checker is optional for the GPU number
             line["cpu_baseline"] = {"error": str(e)}
     r.close()
+    if rank == 0 and ws == 1 and not args.no_cache:
+        try:
+            line["radiance_cache"] = radiance_cache_leg(pt)
+        except Exception as e:
+            line["radiance_cache"] = {"error": f"{type(e).__name__}: {e}"}
     if rank == 0 and ws == 1 and not args.no_serving:
         try:
             line["serving"] = serving_leg(n_jobs=args.serving_jobs)

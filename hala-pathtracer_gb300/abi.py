@@ -113,7 +113,7 @@ class CacheConfig(C.Structure):
     _fields_ = [("query_depth", C.c_uint32), ("train_shift", C.c_uint32), ("batch_size", C.c_uint32),
                 ("log2_table_size", C.c_uint32), ("learning_rate", C.c_float),
                 ("min_resolution", C.c_uint32), ("max_resolution", C.c_uint32), ("seed", C.c_uint32),
-                ("warmup_frames", C.c_uint32)]
+                ("warmup_frames", C.c_uint32), ("paths_per_pass", C.c_uint32), ("steps_per_pass", C.c_uint32)]
 
 
 class ServerConfig(C.Structure):

@@ -669,10 +669,11 @@ pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) {
   r->stats.render_ms = 0.0;
   if (total == 0) return PT_OK;
   uint64_t want = r->cfg.wave_paths ? r->cfg.wave_paths : (1u << 25);
+  if (r->cache_on) want = std::min<uint64_t>(want, r->cache_cfg.paths_per_pass);
   uint32_t cap = (uint32_t)std::min<uint64_t>(want, total);
   const bool med = (r->features & PT_FEATURE_MEDIUM) != 0;
   CK(r, r->W.ensure(cap, med, false));
-  cap = r->W.cap;
+  if (!r->cache_on) cap = r->W.cap;  // a larger wavefront already allocated costs nothing more
   cudaStream_t st = r->stream;
   const uint64_t g_start = r->frame_index * WH;
   if (r->cfg.keep_samples) {
@@ -800,6 +801,8 @@ pt_status pt_renderer_set_radiance_cache(pt_renderer* r, const pt_cache_config* 
   if (cfg->learning_rate > 0.0f) c.learning_rate = cfg->learning_rate;
   if (cfg->min_resolution) c.min_resolution = cfg->min_resolution;
   if (cfg->max_resolution) c.max_resolution = cfg->max_resolution;
+  if (cfg->paths_per_pass) c.paths_per_pass = cfg->paths_per_pass;
+  c.steps_per_pass = cfg->steps_per_pass;
   c.seed = cfg->seed;
   if (c.query_depth == 0) return fail(r, PT_ERR_INVALID_ARG, "query_depth must be at least 1");
   if (c.train_shift > 16) return fail(r, PT_ERR_INVALID_ARG, "train_shift must be at most 16");

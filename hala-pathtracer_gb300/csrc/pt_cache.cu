@@ -40,7 +40,8 @@ constexpr int WSTRIDE5 = 24;  // smem row stride of the 16-wide backward rows of
 constexpr int SMEM_WN = 5 * 64 * WSTRIDE + NC_OUT * WSTRIDE;   // forward weights (bf16 elements)
 constexpr int SMEM_WK = 5 * 64 * WSTRIDE + 64 * WSTRIDE5;      // backward weights
 constexpr int TILE = 16 * WSTRIDE;                               // one warp's 16-row staging tile
-constexpr int CACHE_WARPS = 4;
+constexpr int CACHE_WARPS = 4;  // training kernels (255 registers per thread)
+constexpr int INFER_WARPS = 8;  // more warps hide the latency of the hash-table gathers
 constexpr uint32_t HASH_P1 = 2654435761u, HASH_P2 = 805459861u;
 
 __device__ __forceinline__ int wn_smem_off(int l) { return l * 64 * WSTRIDE; }
@@ -265,19 +266,19 @@ __device__ __forceinline__ void mlp_forward(const __nv_bfloat16* wn_sm, uint32_t
   layer_fwd<2>(a, wn_sm + wn_smem_off(NC_LAYERS - 1), out, g, t);
 }
 
-__global__ void __launch_bounds__(CACHE_WARPS * 32) k_cache_infer(CacheView V, const float4* rec, const uint32_t* idx,
+__global__ void __launch_bounds__(INFER_WARPS * 32) k_cache_infer(CacheView V, const float4* rec, const uint32_t* idx,
                                                                  const uint32_t* count_dev, uint32_t n_max,
                                                                  float4* out, const float4* scale) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __nv_bfloat16* wn_sm = reinterpret_cast<__nv_bfloat16*>(smem_raw);
   __nv_bfloat16* tiles = wn_sm + SMEM_WN;
   const uint32_t n = count_dev ? min(*count_dev, n_max) : n_max;
-  if ((uint32_t)blockIdx.x * CACHE_WARPS * 16 >= n) return;
+  if ((uint32_t)blockIdx.x * INFER_WARPS * 16 >= n) return;
   load_wn(V, wn_sm);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   __nv_bfloat16* X = tiles + warp * TILE;
-  for (uint32_t tile = blockIdx.x * CACHE_WARPS + warp; tile * 16 < n; tile += gridDim.x * CACHE_WARPS) {
+  for (uint32_t tile = blockIdx.x * INFER_WARPS + warp; tile * 16 < n; tile += gridDim.x * INFER_WARPS) {
     const uint32_t row0 = tile * 16;
     {
       uint32_t r = row0 + (lane & 15);
@@ -618,7 +619,7 @@ __global__ void k_cache_init_grid(float* w, uint64_t count, uint64_t seed, float
   if (i < count) w[i] = scale * init_uniform(seed, i);
 }
 
-constexpr size_t SMEM_INFER = (size_t)(SMEM_WN + CACHE_WARPS * TILE) * 2;
+constexpr size_t SMEM_INFER = (size_t)(SMEM_WN + INFER_WARPS * TILE) * 2;
 constexpr size_t SMEM_TRAIN = (size_t)(SMEM_WN + SMEM_WK + CACHE_WARPS * TILE) * 2;
 constexpr uint32_t DW_ROWS_PER_BLOCK = 512;
 
@@ -633,8 +634,8 @@ void launch_cache_infer(const CacheView& V, const float4* rec, const uint32_t* i
   }
   if (n_max == 0) return;
   uint32_t tiles = (n_max + 15) / 16;
-  uint32_t blocks = std::min<uint32_t>((tiles + CACHE_WARPS - 1) / CACHE_WARPS, (uint32_t)device_sm_count() * 4);
-  k_cache_infer<<<blocks, CACHE_WARPS * 32, SMEM_INFER, st>>>(V, rec, idx, count_dev, n_max, out, scale);
+  uint32_t blocks = std::min<uint32_t>((tiles + INFER_WARPS - 1) / INFER_WARPS, (uint32_t)device_sm_count() * 2);
+  k_cache_infer<<<blocks, INFER_WARPS * 32, SMEM_INFER, st>>>(V, rec, idx, count_dev, n_max, out, scale);
 }
 
 }  // namespace hpt
@@ -730,12 +731,17 @@ static cudaError_t train_step(pt_cache* c, const float4* rec, const float4* tgt,
 cudaError_t cache_train_device(pt_cache* c, const float4* rec, const float4* tgt, uint32_t n, cudaStream_t st,
                                uint32_t* steps_done) {
   uint32_t steps = 0;
-  const uint32_t B = c->cfg.batch_size;
-  for (uint32_t off = 0; off < n; off += B) {
-    uint32_t m = std::min(B, n - off);
-    cudaError_t e = train_step(c, rec + (size_t)off * 4, tgt + off, m, st);
-    if (e != cudaSuccess) return e;
-    ++steps;
+  if (n > 0) {
+    const uint32_t B = c->cfg.batch_size;
+    const uint32_t batches = (n + B - 1) / B;
+    const uint32_t total = std::max(batches, c->cfg.steps_per_pass);
+    for (uint32_t k = 0; k < total; ++k) {
+      const uint32_t off = (k % batches) * B;
+      const uint32_t m = std::min(B, n - off);
+      cudaError_t e = train_step(c, rec + (size_t)off * 4, tgt + off, m, st);
+      if (e != cudaSuccess) return e;
+      ++steps;
+    }
   }
   if (steps_done) *steps_done = steps;
   return cudaSuccess;
@@ -771,6 +777,8 @@ void pt_cache_config_default(pt_cache_config* c) {
   c->max_resolution = 2048;
   c->seed = 1;
   c->warmup_frames = 1;
+  c->paths_per_pass = 1u << 20;
+  c->steps_per_pass = 4;
 }
 
 pt_status pt_cache_create(const pt_cache_config* cfg, pt_cache** out) {
@@ -979,10 +987,17 @@ pt_status pt_cache_train(pt_cache* c, const float* records, const float* targets
   pt_status s = upload_rows(c, records, targets, n);
   if (s != PT_OK) return s;
   cudaStream_t st = c->stream;
+  const uint32_t keep = c->cfg.steps_per_pass;
+  c->cfg.steps_per_pass = 0;
   for (uint32_t k = 0; k < steps; ++k) {
     uint32_t done = 0;
-    CCK(c, cache_train_device(c, c->rec.p, c->tgt.p, n, st, &done));
+    cudaError_t e = cache_train_device(c, c->rec.p, c->tgt.p, n, st, &done);
+    if (e != cudaSuccess) {
+      c->cfg.steps_per_pass = keep;
+      CCK(c, e);
+    }
   }
+  c->cfg.steps_per_pass = keep;
   if (last_loss) CCK(c, cudaMemcpyAsync(last_loss, c->loss.p, sizeof(float), cudaMemcpyDeviceToHost, st));
   CCK(c, cudaStreamSynchronize(st));
   return PT_OK;

@@ -140,6 +140,12 @@ __global__ void __launch_bounds__(256) k_trace(const __grid_constant__ DevScene 
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     uint32_t p = Q.in[i];
     const DevScene& S = MULTI ? P.jobs[P.job[p]] : S0;
+    if (P.c_train) {
+      // a training path leaving the cache vertex: what it gathered so far is
+      // the part of its radiance the cache does not predict
+      uint32_t k = P.c_train[p];
+      if (k != 0xFFFFFFFFu && P.depth[p] == P.c_depth + 1u) P.t_R[k] = P.rad[p];
+    }
     float4 o4 = P.ray_o[p], d4 = P.ray_d[p];
     HitRec h = trace_closest<BRUTE, COUNT>(S, f3(o4), f3(d4), 0.0f, WORLD_SIZE, &tc);
     P.hit[p] = make_float4(h.t, h.u, h.v, __uint_as_float(h.id));
@@ -549,33 +555,36 @@ __global__ void __launch_bounds__(256) k_shade(const __grid_constant__ DevScene 
     const pt_material& mat = S.mats[st.mat];
     st.fr.eta = dot(d, st.normal) < 0.0f ? (1.0f / mat.ior) : mat.ior;
     st.fr.depth = depth;
+    // Radiance-cache vertex: its emission and direct light are computed as
+    // usual; the light arriving through the BSDF continuation (indirect) is
+    // either the cache's estimate -- the path ends here and the estimate is
+    // added after the bounce loop -- or, for a training path, traced on.
+    bool cache_query = false;
     if (CACHE && depth == P.c_depth) {
-      // radiance-cache vertex: the path either ends here with the cache's
-      // estimate (added after the bounce loop) or continues as a training path
       const float4 rec0 = make_float4(st.fhp.x, st.fhp.y, st.fhp.z, -d.x);
       const float4 rec1 = make_float4(-d.y, -d.z, st.ffnormal.x, st.ffnormal.y);
       const float4 rec2 = make_float4(st.ffnormal.z, mat.base_color[0], mat.base_color[1], mat.base_color[2]);
       const float4 rec3 = make_float4(mat.roughness, mat.metallic, mat.specular_transmission, 0.0f);
       const bool train = P.c_mode == 1 || P.c_shift == 0 || ((p * 2654435761u) >> (32u - P.c_shift)) == 0u;
       if (!train) {
+        cache_query = true;
         P.c_rec[4 * (size_t)p] = rec0;
         P.c_rec[4 * (size_t)p + 1] = rec1;
         P.c_rec[4 * (size_t)p + 2] = rec2;
         P.c_rec[4 * (size_t)p + 3] = rec3;
         P.c_T[p] = make_float4(T.x, T.y, T.z, 0.0f);
-        queue_push(P.c_queue, &P.c_counts[0], p, true);
-        continue;
-      }
-      const bool fresh = P.c_train[p] == 0xFFFFFFFFu;
-      uint32_t k = append_index(&P.c_counts[1], fresh);
-      if (fresh) {
-        P.t_rec[4 * (size_t)k] = rec0;
-        P.t_rec[4 * (size_t)k + 1] = rec1;
-        P.t_rec[4 * (size_t)k + 2] = rec2;
-        P.t_rec[4 * (size_t)k + 3] = rec3;
-        P.t_T[k] = make_float4(T.x, T.y, T.z, 0.0f);
-        P.t_R[k] = make_float4(rad.x, rad.y, rad.z, 0.0f);
-        P.c_train[p] = k;
+      } else {
+        const bool fresh = P.c_train[p] == 0xFFFFFFFFu;
+        uint32_t k = append_index(&P.c_counts[1], fresh);
+        if (fresh) {
+          P.t_rec[4 * (size_t)k] = rec0;
+          P.t_rec[4 * (size_t)k + 1] = rec1;
+          P.t_rec[4 * (size_t)k + 2] = rec2;
+          P.t_rec[4 * (size_t)k + 3] = rec3;
+          P.t_T[k] = make_float4(T.x, T.y, T.z, 0.0f);
+          P.t_R[k] = make_float4(__int_as_float(0x7FC00000), 0.0f, 0.0f, 0.0f);
+          P.c_train[p] = k;
+        }
       }
     }
     if (depth == 0) {
@@ -672,6 +681,12 @@ __global__ void __launch_bounds__(256) k_shade(const __grid_constant__ DevScene 
             P.sh_T[p] = make_float4(T.x, T.y, T.z, 0.0f);
           }
         }
+        if (CACHE && cache_query) {
+          queue_push(P.c_queue, &P.c_counts[0], p, true);
+          stop = true;
+        }
+      }
+      if (!(CACHE && cache_query) && !skip) {
         float3 L;
         float pdf;
         uint32_t sflags = 0;
@@ -821,13 +836,18 @@ __global__ void k_accumulate(PathState P, uint64_t g0, uint32_t n, uint32_t WH, 
 }
 
 // Training targets of the radiance cache: what the unbiased path gathered
-// from the cache vertex on, divided by the throughput arriving there.
+// after leaving the cache vertex (its indirect light there), divided by the
+// throughput arriving at the vertex; zero when the path ended at the vertex.
 __global__ void k_cache_targets(PathState P, uint32_t n, float4* tgt) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   uint32_t k = P.c_train[i];
   if (k == 0xFFFFFFFFu) return;
   float4 r = P.rad[i], R = P.t_R[k], T = P.t_T[k];
+  if (R.x != R.x) {
+    tgt[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    return;
+  }
   float3 y = make_float3(T.x > 0.0f ? (r.x - R.x) / T.x : 0.0f, T.y > 0.0f ? (r.y - R.y) / T.y : 0.0f,
                          T.z > 0.0f ? (r.z - R.z) / T.z : 0.0f);
   tgt[k] = make_float4(fmaxf(y.x, 0.0f), fmaxf(y.y, 0.0f), fmaxf(y.z, 0.0f), 0.0f);

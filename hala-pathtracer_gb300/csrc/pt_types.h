@@ -115,7 +115,8 @@ struct PathState {
   uint32_t* c_train;   // training-sample index of the slot, ~0u = none
   float4* t_rec;       // training samples: record (4 float4 each),
   float4* t_T;         //   throughput arriving at the vertex,
-  float4* t_R;         //   radiance gathered before the vertex
+  float4* t_R;         //   radiance gathered up to the vertex's own emission and
+                       //   direct light (NaN until the path leaves the vertex)
   uint32_t c_depth;    // vertex index of the query
   uint32_t c_mode;     // 1 = every path trains (warm-up), 2 = query, 1 in 2^c_shift trains
   uint32_t c_shift;

@@ -429,10 +429,12 @@ pt_status pt_server_get_stats(pt_server* s, pt_server_stats* out);
  * 2^log2_table_size fp16 entries of 2 features per level) plus direction,
  * normal and material inputs, feeding an MLP with 5 hidden layers of 64 ReLU
  * units (BF16 weights, FP32 accumulation), trained with Adam on the relative
- * L2 loss. With a cache attached to a renderer, paths end at vertex
- * `query_depth` and take the cache's estimate of the radiance leaving that
- * vertex; 1 in 2^train_shift paths continue unbiased and become training
- * samples. Without a cache the renderer is the plain tracer.
+ * L2 loss. With a cache attached to a renderer, the vertex `query_depth` of
+ * a path gets its emission and direct light as usual, and the light arriving
+ * there through further bounces (the indirect part) is the cache's estimate:
+ * the path ends at that vertex. 1 in 2^train_shift paths continue unbiased
+ * and become training samples. Without a cache the renderer is the plain
+ * tracer.
  *
  * Query record (16 floats): position xyz, outgoing direction xyz (towards
  * the previous vertex), shading normal xyz, base colour rgb, roughness,
@@ -449,10 +451,15 @@ typedef struct pt_cache_config {
   uint32_t max_resolution;  /* finest grid level */
   uint32_t seed;            /* weight initialisation */
   uint32_t warmup_frames;   /* frames traced with every path training before the first query */
+  uint32_t paths_per_pass;  /* wavefront size while a cache is attached: the cache trains
+                               between wavefronts, so smaller passes adapt sooner */
+  uint32_t steps_per_pass;  /* optimiser steps after each pass at least (batches cycle
+                               through the pass's samples) */
 } pt_cache_config;
 
 /* query_depth 1, 1/16 training paths, batch 65536, 2^19 entries, lr 1e-2,
- * resolutions 16..2048, seed 1, one warm-up frame. */
+ * resolutions 16..2048, seed 1, one warm-up frame, passes of 2^20 paths,
+ * at least 4 steps per pass. */
 void pt_cache_config_default(pt_cache_config* config);
 pt_status pt_cache_create(const pt_cache_config* config, pt_cache** out);
 void pt_cache_destroy(pt_cache* cache);
