@@ -439,6 +439,12 @@ void pt_material_preprocess(pt_material* m) {
 }
 
 pt_status pt_renderer_create(const pt_tracer_config* cfg, pt_renderer** out) {
+  return renderer_create_with_priority(cfg, 0, out);
+}
+
+}  // extern "C"
+
+pt_status hpt::renderer_create_with_priority(const pt_tracer_config* cfg, int priority, pt_renderer** out) {
   if (!cfg || !out) return PT_ERR_INVALID_ARG;
   *out = nullptr;
   pt_status cs = validate_tracer_config(cfg, nullptr);
@@ -447,13 +453,14 @@ pt_status pt_renderer_create(const pt_tracer_config* cfg, pt_renderer** out) {
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PT_ERR_CUDA;
   pt_renderer* r = new pt_renderer();
   r->cfg = *cfg;
-  if (cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking) != cudaSuccess ||
+  if (cudaStreamCreateWithPriority(&r->stream, cudaStreamNonBlocking, priority) != cudaSuccess ||
       cudaEventCreate(&r->ev0) != cudaSuccess || cudaEventCreate(&r->ev1) != cudaSuccess ||
       cudaMallocHost(&r->pinned, 64) != cudaSuccess) {
     pt_renderer_destroy(r);
     return PT_ERR_CUDA;
   }
   size_t WH = (size_t)cfg->width * cfg->height;
+  AllocScope as(r->stream);
   if (r->accum.ensure(WH) || r->albedo.ensure(WH) || r->normal.ensure(WH) || r->final_img.ensure(WH)) {
     pt_renderer_destroy(r);
     return PT_ERR_OOM;
@@ -465,6 +472,8 @@ pt_status pt_renderer_create(const pt_tracer_config* cfg, pt_renderer** out) {
   *out = r;
   return PT_OK;
 }
+
+extern "C" {
 
 void pt_renderer_destroy(pt_renderer* r) {
   if (!r) return;
@@ -483,6 +492,7 @@ const char* pt_renderer_last_error(const pt_renderer* r) { return r ? r->err.c_s
 
 pt_status pt_renderer_set_scene(pt_renderer* r, const pt_scene_desc* s) {
   if (!r) return PT_ERR_INVALID_ARG;
+  AllocScope alloc_scope(r->stream);
   {
     std::string why;
     pt_status vs = validate_scene_desc(s, &why);
@@ -551,6 +561,7 @@ pt_status pt_renderer_set_scene(pt_renderer* r, const pt_scene_desc* s) {
 
 pt_status pt_renderer_set_envmap(pt_renderer* r, const float* rgb, uint32_t w, uint32_t h, float rot_deg) {
   if (!r) return PT_ERR_INVALID_ARG;
+  AllocScope alloc_scope(r->stream);
   r->committed = false;
   if (!rgb || w == 0 || h == 0) {
     r->env_map = false;
@@ -603,6 +614,7 @@ pt_status pt_renderer_set_camera_index(pt_renderer* r, uint32_t i) {
 
 pt_status pt_renderer_commit(pt_renderer* r) {
   if (!r) return PT_ERR_INVALID_ARG;
+  AllocScope alloc_scope(r->stream);
   if (!r->has_scene) return fail(r, PT_ERR_STATE, "set_scene must come before commit");
   // feature permutation, src/bin/hala-pathtracer.rs:101-114
   uint32_t f = 0;
@@ -656,6 +668,7 @@ pt_status pt_renderer_commit(pt_renderer* r) {
 
 pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) {
   if (!r) return PT_ERR_INVALID_ARG;
+  AllocScope alloc_scope(r->stream);
   if (!r->committed) return fail(r, PT_ERR_STATE, "commit must come before render");
   uint64_t nf = frames;
   if (r->cfg.max_samples > 0) {
@@ -919,6 +932,7 @@ pt_status pt_renderer_get_stream(const pt_renderer* r, void** stream) {
 pt_status pt_renderer_trace_rays(pt_renderer* r, const float* rays, uint32_t n, int32_t any_hit, int32_t brute,
                                  uint32_t* hits) {
   if (!r) return PT_ERR_INVALID_ARG;
+  AllocScope alloc_scope(r->stream);
   if (!r->committed) return fail(r, PT_ERR_STATE, "commit must come before trace_rays");
   if (n == 0) return PT_OK;
   if (!rays || !hits) return fail(r, PT_ERR_INVALID_ARG, "null ray or hit buffer");

@@ -293,12 +293,18 @@ __global__ void k_reorder(const uint32_t* final_ids, uint32_t n, const float4* v
   out[3 * s + 2] = e2[id];
 }
 
+// Build scratch from the stream-ordered allocator of the build stream: no
+// allocation or free here waits for work on other streams.
 template <class T>
 struct Tmp {
   T* p = nullptr;
-  cudaError_t alloc(size_t n) { return cudaMalloc(&p, n * sizeof(T)); }
+  cudaStream_t s = nullptr;
+  cudaError_t alloc(size_t n, cudaStream_t st) {
+    s = st;
+    return cudaMallocAsync(reinterpret_cast<void**>(&p), n * sizeof(T), st);
+  }
   ~Tmp() {
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, s);
   }
 };
 
@@ -312,8 +318,9 @@ int build_bvh(const float4* tri_v0, const float4* tri_e1, const float4* tri_e2, 
   Tmp<BuildTask> tasks_a, tasks_b;
   Tmp<BuildNode> nodes;
   const uint32_t cap = 2 * n;
-  if (tlo.alloc(n) || thi.alloc(n) || tc.alloc(n) || ids_a.alloc(n) || ids_b.alloc(n) || final_ids.alloc(n) ||
-      counters.alloc(4) || tasks_a.alloc(n + 1) || tasks_b.alloc(n + 1) || nodes.alloc(cap))
+  if (tlo.alloc(n, st) || thi.alloc(n, st) || tc.alloc(n, st) || ids_a.alloc(n, st) || ids_b.alloc(n, st) ||
+      final_ids.alloc(n, st) || counters.alloc(4, st) || tasks_a.alloc(n + 1, st) || tasks_b.alloc(n + 1, st) ||
+      nodes.alloc(cap, st))
     return 2;
   k_prep<<<(n + 255) / 256, 256, 0, st>>>(tri_v0, tri_e1, tri_e2, n, tlo.p, thi.p, tc.p, ids_a.p);
   // counters: [0] node counter, [1] task count A, [2] task count B

@@ -12,24 +12,50 @@
 
 namespace hpt {
 
+// Stream on which Buf allocates and frees (stream-ordered allocator) on
+// this host thread; null = plain cudaMalloc/cudaFree. cudaFree waits for the
+// whole device, so a thread that uploads a scene while another thread's
+// wavefronts run allocates through a scope on its own stream instead.
+inline thread_local cudaStream_t tl_alloc_stream = nullptr;
+struct AllocScope {
+  cudaStream_t prev;
+  explicit AllocScope(cudaStream_t s) : prev(tl_alloc_stream) { tl_alloc_stream = s; }
+  ~AllocScope() { tl_alloc_stream = prev; }
+  AllocScope(const AllocScope&) = delete;
+  AllocScope& operator=(const AllocScope&) = delete;
+};
+
 template <class T>
 struct Buf {
   T* p = nullptr;
   size_t n = 0;
+  cudaStream_t s = nullptr;  // stream of a stream-ordered allocation
+  bool pooled = false;
   Buf() = default;
   Buf(const Buf&) = delete;
   Buf& operator=(const Buf&) = delete;
   ~Buf() { release(); }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      if (pooled) cudaFreeAsync(p, s);
+      else cudaFree(p);
+    }
     p = nullptr;
     n = 0;
+    pooled = false;
   }
   cudaError_t ensure(size_t count) {
     if (count <= n && p) return cudaSuccess;
     release();
     if (count == 0) return cudaSuccess;
-    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    cudaError_t e;
+    if (tl_alloc_stream) {
+      e = cudaMallocAsync(reinterpret_cast<void**>(&p), count * sizeof(T), tl_alloc_stream);
+      pooled = e == cudaSuccess;
+      s = tl_alloc_stream;
+    } else {
+      e = cudaMalloc(&p, count * sizeof(T));
+    }
     if (e == cudaSuccess) n = count;
     else p = nullptr;
     return e;
@@ -139,6 +165,9 @@ namespace hpt {
 void renderer_drop_build_inputs(pt_renderer* r);
 // Frees everything of a finished render but its four images.
 void renderer_drop_scene(pt_renderer* r);
+// pt_renderer_create with a stream priority (cudaStreamCreateWithPriority;
+// lower numbers run first).
+pt_status renderer_create_with_priority(const pt_tracer_config* cfg, int priority, pt_renderer** out);
 // Checks of set_scene / HalaRenderer::new; `why` receives the reason.
 pt_status validate_scene_desc(const pt_scene_desc* desc, std::string* why);
 pt_status validate_tracer_config(const pt_tracer_config* config, std::string* why);

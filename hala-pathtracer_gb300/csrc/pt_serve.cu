@@ -196,7 +196,10 @@ pt_status admit_job(pt_server* s, Job& j, std::string& why) {
   c.keep_samples = 0;
   c.wave_paths = 1;
   pt_renderer* r = nullptr;
-  pt_status ps = pt_renderer_create(&c, &r);
+  // uploads and BVH builds of admitted jobs go ahead of the running wavefronts
+  int least = 0, greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&least, &greatest);
+  pt_status ps = renderer_create_with_priority(&c, greatest, &r);
   if (ps != PT_OK) {
     why = "renderer creation failed";
     return ps;
