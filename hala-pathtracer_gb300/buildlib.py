@@ -37,7 +37,7 @@ def headers():
 
 # Shading code is compiled without multiply-add contraction so it rounds like
 # the CPU oracle (explicit fmaf calls are still fused).
-PER_FILE_FLAGS = {"pt_render.cu": ["-fmad=false"]}
+PER_FILE_FLAGS = {f: ["-fmad=false"] for f in ("pt_render.cu", "pt_shade_single.cu", "pt_shade_multi.cu")}
 
 
 def _compile(src, verbose_ptxas=False):

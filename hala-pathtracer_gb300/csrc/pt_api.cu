@@ -152,6 +152,11 @@ pt_status validate_scene_desc(const pt_scene_desc* s, std::string* why) {
   if (s->num_materials && !s->materials) return bad(PT_ERR_INVALID_ARG, "materials is null");
   if (s->num_lights && !s->lights) return bad(PT_ERR_INVALID_ARG, "lights is null");
   if (s->num_textures && !s->textures) return bad(PT_ERR_INVALID_ARG, "textures is null");
+  for (uint32_t i = 0; i < s->num_textures; ++i) {
+    const pt_texture& t = s->textures[i];
+    if (t.width == 0 || t.height == 0 || !t.rgba) return bad(PT_ERR_INVALID_ARG, "empty texture");
+    if ((uint64_t)t.width * t.height > (1ull << 28)) return bad(PT_ERR_UNSUPPORTED, "texture larger than 2^28 texels");
+  }
   uint64_t nv = 0, nt = 0;
   for (uint32_t i = 0; i < s->num_primitives; ++i) {
     const pt_primitive& p = s->primitives[i];
@@ -204,6 +209,8 @@ void renderer_drop_scene(pt_renderer* r) {
   r->env.release();
   r->alias_rows.release();
   r->alias_cols.release();
+  r->tex_texels.release();
+  r->tex_info.release();
   r->committed = false;
   r->has_scene = false;
 }
@@ -221,6 +228,7 @@ uint64_t renderer_estimate_bytes(const pt_scene_desc* d, uint32_t width, uint32_
   // vertex ids 12 + material 4; the BVH build's scratch is about 64 B more
   uint64_t b = V * 100 + T * (252 + 64);
   b += (uint64_t)d->num_materials * sizeof(pt_material) + 4096;
+  for (uint32_t i = 0; i < d->num_textures; ++i) b += 16ull * d->textures[i].width * d->textures[i].height + 16;
   const uint64_t E = (uint64_t)env_w * env_h;
   b += E * (16 + 8 + 16 + 8) + (uint64_t)env_h * 16;
   b += (uint64_t)width * height * (3 * 16 + 4);
@@ -318,6 +326,9 @@ void fill_view(pt_renderer* r) {
   S.rr_depth = r->cfg.rr_depth;
   S.seed = r->cfg.seed;
   S.features = r->features;
+  S.tex_texels = r->tex_texels.p;
+  S.tex_info = r->tex_info.p;
+  S.num_textures = r->num_textures;
 }
 
 bool write_pfm(const char* path, const float4* px, uint32_t w, uint32_t h) {
@@ -550,6 +561,24 @@ pt_status pt_renderer_set_scene(pt_renderer* r, const pt_scene_desc* s) {
   if (!r->mats.empty())
     CK(r, cudaMemcpyAsync(r->dmats.p, r->mats.data(), r->mats.size() * sizeof(pt_material), cudaMemcpyHostToDevice,
                           st));
+  {
+    // material textures, back to back (texels are RGBA32F already)
+    std::vector<uint4> info(s->num_textures);
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < s->num_textures; ++i) {
+      info[i] = make_uint4((uint32_t)total, s->textures[i].width, s->textures[i].height, 0u);
+      total += (uint64_t)s->textures[i].width * s->textures[i].height;
+    }
+    if (total >= (1ull << 32)) return fail(r, PT_ERR_UNSUPPORTED, "more than 2^32 texels in all textures");
+    r->num_textures = s->num_textures;
+    CK(r, r->tex_info.ensure(std::max<size_t>(info.size(), 1)));
+    CK(r, r->tex_texels.ensure(std::max<uint64_t>(total, 1)));
+    if (!info.empty())
+      CK(r, cudaMemcpyAsync(r->tex_info.p, info.data(), info.size() * sizeof(uint4), cudaMemcpyHostToDevice, st));
+    for (uint32_t i = 0; i < s->num_textures; ++i)
+      CK(r, cudaMemcpyAsync(r->tex_texels.p + info[i].x, s->textures[i].rgba,
+                            sizeof(float4) * (size_t)info[i].y * info[i].z, cudaMemcpyHostToDevice, st));
+  }
   launch_flatten(r->raw_verts.p, r->raw_idx.p, r->dprims.p, (uint32_t)prims.size(), r->nverts, r->ntris, nullptr,
                  nullptr, r->vnorm.p, r->vtan.p, r->vuv.p, r->wpos.p, r->tri_v0.p, r->tri_e1.p, r->tri_e2.p,
                  r->tri_vidx.p, r->tri_mat.p, st);
@@ -621,6 +650,9 @@ pt_status pt_renderer_commit(pt_renderer* r) {
   for (const pt_material& m : r->mats) {
     if (m.medium.type != PT_MEDIUM_NONE) f |= PT_FEATURE_MEDIUM | PT_FEATURE_VOL_MIS;
     if (m.opacity < 1.0f) f |= PT_FEATURE_TRANSPARENT;
+    if (m.base_color_map_index < r->num_textures || m.normal_map_index < r->num_textures ||
+        m.metallic_roughness_map_index < r->num_textures || m.emission_map_index < r->num_textures)
+      f |= PT_FEATURE_TEXTURED;
   }
   r->features = f;
   cudaStream_t st = r->stream;

@@ -585,7 +585,7 @@ __device__ __forceinline__ LobeProbs lobe_probs(const pt_material& m, float eta,
 }
 
 // disney.glsl:264-390 (ROUGHNESS_REGULARIZE_EVAL)
-__device__ __noinline__ float3 disney_eval(bool ans, const ShadeFrame& s, const pt_material& m, float3 V,
+static __device__ __noinline__ float3 disney_eval(bool ans, const ShadeFrame& s, const pt_material& m, float3 V,
                                            float3 N, float3 L, float& pdf) {
   float ax = m.ax, ay = m.ay;
   if (s.depth > 0 && ans) {

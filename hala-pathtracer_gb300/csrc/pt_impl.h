@@ -120,6 +120,9 @@ struct pt_renderer {
   hpt::Buf<float2> vuv;
   hpt::Buf<uint32_t> tri_vidx, tri_mat;
   hpt::Buf<pt_material> dmats;
+  hpt::Buf<float4> tex_texels;
+  hpt::Buf<uint4> tex_info;
+  uint32_t num_textures = 0;
 
   // environment
   bool env_map = false;

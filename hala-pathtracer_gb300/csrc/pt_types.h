@@ -80,6 +80,11 @@ struct DevScene {
   // tracer settings, MainUBO inc/global.glsl:11-30
   uint32_t width, height, max_depth, rr_depth, seed;
   uint32_t features;
+  // material textures (g_textures, inc/global.glsl:48): texels of all maps
+  // back to back, and per map (first texel, width, height, 0)
+  const float4* tex_texels;
+  const uint4* tex_info;
+  uint32_t num_textures;
 };
 
 // Structure-of-arrays path state of one wavefront (capacity P paths).

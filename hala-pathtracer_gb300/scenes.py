@@ -369,11 +369,16 @@ class Scene:
         self.width, self.height = 256, 256
         self.spp, self.max_depth, self.rr_depth, self.seed = 16, 8, 0, 0
         self.tonemap = (True, True, False)
+        self.textures = []       # (H, W, 4) float32 RGBA, linear values
         self._keep = []
 
     def add_material(self, m):
         self.materials.append(m)
         return len(self.materials) - 1
+
+    def add_texture(self, rgba):
+        self.textures.append(np.ascontiguousarray(rgba, np.float32))
+        return len(self.textures) - 1
 
     def add_mesh(self, verts, idx, mat, transform=None):
         tr = IDENTITY if transform is None else np.asarray(transform, np.float32)
@@ -412,8 +417,13 @@ class Scene:
         d.materials, d.num_materials = mats, len(self.materials)
         d.lights, d.num_lights = lights, len(self.lights)
         d.cameras, d.num_cameras = cams, len(self.cameras)
-        d.textures, d.num_textures = None, 0
-        self._keep = [prims, mats, lights, cams, keep]
+        texs = (abi.Texture * max(1, len(self.textures)))()
+        for k, t in enumerate(self.textures):
+            texs[k].rgba = t.ctypes.data_as(C.POINTER(C.c_float))
+            texs[k].height, texs[k].width = t.shape[0], t.shape[1]
+            keep.append(t)
+        d.textures, d.num_textures = texs, len(self.textures)
+        self._keep = [prims, mats, lights, cams, texs, keep]
         return d
 
     def env_pointer(self):
@@ -550,6 +560,39 @@ def media_box(width=1024, height=1024, spp=128, max_depth=32, rr_depth=4, seed=0
                                   medium=(abi.MEDIUM_ABSORB, (0.0, 0.0, 0.0), 0.02, 0.0)))
     s.add_mesh(*box_mesh((0.5, 0.5, 0.5), (0.99, 0.99, 0.98), 0.0), fog)
     return s
+
+
+# --------------------------------------------------------------------------- textures
+
+def checker_texture(size=32, cells=8, c0=(0.9, 0.85, 0.75), c1=(0.15, 0.2, 0.35)):
+    """RGBA checkerboard with a gentle gradient (so bilinear filtering shows)."""
+    y, x = np.mgrid[0:size, 0:size]
+    on = ((x * cells // size) + (y * cells // size)) % 2 == 0
+    rgb = np.where(on[..., None], np.asarray(c0), np.asarray(c1))
+    rgb = rgb * (0.75 + 0.25 * (x / max(1, size - 1)))[..., None]
+    return np.concatenate([rgb, np.ones((size, size, 1))], -1).astype(np.float32)
+
+
+def bump_normal_map(size=32, seed=5, strength=0.6):
+    """Tangent-space normal map (RGB in [0,1]) of a smooth random height field."""
+    rng = np.random.default_rng(seed)
+    h = rng.normal(size=(size // 4, size // 4))
+    h = np.kron(h, np.ones((4, 4)))
+    for _ in range(2):
+        h = 0.25 * (np.roll(h, 1, 0) + np.roll(h, -1, 0) + np.roll(h, 1, 1) + np.roll(h, -1, 1))
+    gx = (np.roll(h, -1, 1) - np.roll(h, 1, 1)) * strength
+    gy = (np.roll(h, -1, 0) - np.roll(h, 1, 0)) * strength
+    n = np.stack([-gx, -gy, np.ones_like(gx)], -1)
+    n /= np.linalg.norm(n, axis=-1, keepdims=True)
+    return np.concatenate([n * 0.5 + 0.5, np.ones((size, size, 1))], -1).astype(np.float32)
+
+
+def metallic_roughness_texture(size=16):
+    """glTF layout: G = roughness (left to right), B = metallic (bottom to top)."""
+    y, x = np.mgrid[0:size, 0:size]
+    r = 0.05 + 0.9 * x / (size - 1)
+    m = y / (size - 1)
+    return np.stack([np.zeros_like(r), r, m, np.ones_like(r)], -1).astype(np.float32)
 
 
 def tiny_variants():

@@ -219,6 +219,7 @@ typedef struct pt_stats {
 #define PT_FEATURE_MEDIUM 1u
 #define PT_FEATURE_VOL_MIS 2u
 #define PT_FEATURE_TRANSPARENT 4u
+#define PT_FEATURE_TEXTURED 8u  /* some material uses a texture map */
 
 typedef struct pt_renderer pt_renderer;
 

@@ -725,6 +725,60 @@ static void fill_state(const Ctx& c, const Ray& r, const Hit& h, State& s) {
   s.tex_coord = uv;
 }
 
+// ---------------------------------------------------------------- material textures
+// pathtracer.rgen.glsl:121-145; textureLod with bilinear filtering, repeat
+// wrapping, texel centres at half-integers, row 0 at v = 0 (the glTF default
+// sampler; the reference's sampler object lives in its renderer crate).
+inline uint32_t wrap_texel(long long i, uint32_t n) {
+  long long m = i % (long long)n;
+  return (uint32_t)(m < 0 ? m + n : m);
+}
+static void sample_texture(const Texture& t, float u, float v, float out[4]) {
+  if (!(std::fabs(u) < 1e6f)) u = 0.0f;
+  if (!(std::fabs(v) < 1e6f)) v = 0.0f;
+  const float x = u * (float)t.w - 0.5f, y = v * (float)t.h - 0.5f;
+  const float x0 = std::floor(x), y0 = std::floor(y);
+  const float fx = x - x0, fy = y - y0;
+  const uint32_t ix0 = wrap_texel((long long)x0, t.w), ix1 = wrap_texel((long long)x0 + 1, t.w);
+  const uint32_t iy0 = wrap_texel((long long)y0, t.h), iy1 = wrap_texel((long long)y0 + 1, t.h);
+  const float* a = &t.rgba[4 * ((size_t)iy0 * t.w + ix0)];
+  const float* b = &t.rgba[4 * ((size_t)iy0 * t.w + ix1)];
+  const float* cc = &t.rgba[4 * ((size_t)iy1 * t.w + ix0)];
+  const float* e = &t.rgba[4 * ((size_t)iy1 * t.w + ix1)];
+  for (int k = 0; k < 4; ++k) {
+    float top = a[k] + (b[k] - a[k]) * fx;
+    float bot = cc[k] + (e[k] - cc[k]) * fx;
+    out[k] = top + (bot - top) * fy;
+  }
+}
+
+static void apply_maps(const Ctx& c, Material& m, State& st, const V3& dir) {
+  const uint32_t nt = (uint32_t)c.texs.size();
+  float t[4];
+  if (m.base_color_map < nt) {
+    sample_texture(c.texs[m.base_color_map], st.tex_coord.x, st.tex_coord.y, t);
+    m.base_color = V3(t[0], t[1], t[2]);
+  }
+  if (m.mr_map < nt) {
+    sample_texture(c.texs[m.mr_map], st.tex_coord.x, st.tex_coord.y, t);
+    m.metallic = t[2];
+    m.roughness = t[1];
+  }
+  if (m.emission_map < nt) {
+    sample_texture(c.texs[m.emission_map], st.tex_coord.x, st.tex_coord.y, t);
+    m.emission = V3(t[0], t[1], t[2]);
+  }
+  if (m.normal_map < nt) {
+    sample_texture(c.texs[m.normal_map], st.tex_coord.x, st.tex_coord.y, t);
+    V3 nts(t[0], t[1], t[2] * 5.0f);
+    nts = normalize(nts * 2.0f - V3(1.0f));
+    const V3 orig = st.normal;
+    st.normal = normalize(st.tangent * nts.x + st.bitangent * nts.y + st.normal * nts.z);
+    st.ffnormal = dot(orig, dir) <= 0.0f ? st.normal : -st.normal;
+    st.bitangent = cross(st.normal, st.tangent);
+  }
+}
+
 // ---------------------------------------------------------------- environment
 // Nearest texel of the equirect map at (u, v): u wraps, v clamps, NaN -> 0.
 inline uint32_t env_texel_index(const Ctx& c, float u, float v) {
@@ -1510,6 +1564,7 @@ struct Tracer {
       }
       Material mat = c.mats[st.material_index];
       st.eta = dot(ray.d, st.normal) < 0.0f ? (1.0f / mat.ior) : mat.ior;
+      apply_maps(c, mat, st, ray.d);
       if (st.depth == 0) {
         albedo = mat.base_color;
         normal = st.normal;
@@ -1738,6 +1793,14 @@ int or_set_scene(or_ctx* o, const pt_scene_desc* s) {
   }
   c.mats.clear();
   for (uint32_t i = 0; i < s->num_materials; ++i) c.mats.push_back(to_mat(s->materials[i]));
+  c.texs.assign(s->num_textures, Texture{});
+  for (uint32_t i = 0; i < s->num_textures; ++i) {
+    const pt_texture& t = s->textures[i];
+    if (!t.rgba || t.width == 0 || t.height == 0) return PT_ERR_INVALID_ARG;
+    c.texs[i].w = t.width;
+    c.texs[i].h = t.height;
+    c.texs[i].rgba.assign(t.rgba, t.rgba + 4 * (size_t)t.width * t.height);
+  }
   c.lights.clear();
   for (uint32_t i = 0; i < s->num_lights && i < PT_MAX_LIGHTS; ++i) {
     const pt_light& l = s->lights[i];

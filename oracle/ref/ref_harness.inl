@@ -75,6 +75,10 @@ struct Ctx {
   std::vector<vec4> accum, albedo, normal;
   std::vector<unsigned char> final_img;
   uint64_t frame_index = 0;
+  // material textures behind g_textures (sampler kind 3, id = index)
+  std::vector<std::vector<float>> tex_rgba;
+  std::vector<uint> tex_w, tex_h;
+  std::vector<sampler2D> tex_samplers;
 };
 
 Ctx* g_ctx = nullptr;
@@ -182,7 +186,36 @@ vec4 textureLod(const sampler2D& s, const vec2& uv, float) {
     uint x = alias_draw(&c.prob_cols[(size_t)y * c.env_w], &c.alias_cols[(size_t)y * c.env_w], c.env_w, uv.x, f);
     return vec4(((float)x + f) / (float)c.env_w, 0.0f, 0.0f, 0.0f);
   }
-  return vec4(1.0f, 1.0f, 1.0f, 1.0f);  // material textures are not bound in the parity scenes
+  if (s.kind == 3 && (size_t)s.id < c.tex_rgba.size()) {
+    // material texture: bilinear, repeat, texel centres at half-integers
+    // (the sampler the oracle and the CUDA path define)
+    const uint w = c.tex_w[s.id], h = c.tex_h[s.id];
+    float u = uv.x, v = uv.y;
+    if (!(std::fabs(u) < 1e6f)) u = 0.0f;
+    if (!(std::fabs(v) < 1e6f)) v = 0.0f;
+    const float x = u * (float)w - 0.5f, y = v * (float)h - 0.5f;
+    const float x0 = std::floor(x), y0 = std::floor(y);
+    const float fx = x - x0, fy = y - y0;
+    auto wrap = [](long long i, uint n) {
+      long long m = i % (long long)n;
+      return (uint)(m < 0 ? m + n : m);
+    };
+    const uint ix0 = wrap((long long)x0, w), ix1 = wrap((long long)x0 + 1, w);
+    const uint iy0 = wrap((long long)y0, h), iy1 = wrap((long long)y0 + 1, h);
+    const float* T = c.tex_rgba[s.id].data();
+    const float* a = T + 4 * ((size_t)iy0 * w + ix0);
+    const float* b = T + 4 * ((size_t)iy0 * w + ix1);
+    const float* cc = T + 4 * ((size_t)iy1 * w + ix0);
+    const float* e = T + 4 * ((size_t)iy1 * w + ix1);
+    float o[4];
+    for (int k = 0; k < 4; ++k) {
+      float top = a[k] + (b[k] - a[k]) * fx;
+      float bot = cc[k] + (e[k] - cc[k]) * fx;
+      o[k] = top + (bot - top) * fy;
+    }
+    return vec4(o[0], o[1], o[2], o[3]);
+  }
+  return vec4(1.0f, 1.0f, 1.0f, 1.0f);
 }
 
 vec4 imageLoad(const image2D& img, const ivec2& p) {
@@ -374,6 +407,17 @@ int ref_set_scene(void* h, const pt_scene_desc* s) {
       c.tris.push_back(tr);
     }
   }
+  c.tex_rgba.assign(s->num_textures, {});
+  c.tex_w.assign(s->num_textures, 0);
+  c.tex_h.assign(s->num_textures, 0);
+  c.tex_samplers.clear();
+  for (uint i = 0; i < s->num_textures; ++i) {
+    const pt_texture& t = s->textures[i];
+    c.tex_rgba[i].assign(t.rgba, t.rgba + 4 * (size_t)t.width * t.height);
+    c.tex_w[i] = t.width;
+    c.tex_h[i] = t.height;
+    c.tex_samplers.push_back(sampler2D((int)i, 3));
+  }
   c.mats.assign(s->num_materials, MaterialBuffer{});
   for (uint i = 0; i < s->num_materials; ++i) {
     const pt_material& m = s->materials[i];
@@ -491,6 +535,7 @@ int ref_render(void* h, uint frames, int threads) {
   g_ctx = &c;
   g_materials = c.mats.data();
   g_primitives = c.prims.data();
+  g_textures = c.tex_samplers.data();
   const uint W = c.cfg.width, H = c.cfg.height;
   const uint64_t f0 = c.frame_index;
   std::atomic<uint> next{0};

@@ -86,8 +86,39 @@ def no_tonemap():
     return s
 
 
+def textured():
+    """Every material map: a checker base colour on the floor (uv repeated
+    2.5 times, so the sampler wraps), a normal map on the back wall, a
+    metallic/roughness map on a Disney box, an emission map on a panel."""
+    s = S.cornell(24, 24, 3, max_depth=6, rr_depth=2, seed=0, boxes=False)
+    checker = s.add_texture(S.checker_texture())
+    bumps = s.add_texture(S.bump_normal_map())
+    mr = s.add_texture(S.metallic_roughness_texture())
+    glow = s.add_texture(S.checker_texture(8, 2, (3.0, 2.0, 0.5), (0.0, 0.0, 0.0)))
+    floor = s.materials[0]
+    m_floor = S.material((1, 1, 1))
+    m_floor.base_color_map_index = checker
+    m_wall = S.material((0.7, 0.7, 0.7))
+    m_wall.normal_map_index = bumps
+    m_box = S.material((0.8, 0.5, 0.3), abi.MATERIAL_DISNEY, roughness=0.5)
+    m_box.metallic_roughness_map_index = mr
+    m_glow = S.material((0.2, 0.2, 0.2))
+    m_glow.emission_map_index = glow
+    del floor
+    fi, wi, bi, gi = (s.add_material(m) for m in (m_floor, m_wall, m_box, m_glow))
+    v, i, tr, _ = s.meshes[0]
+    v = v.copy()
+    v[:, 9:11] *= 2.5
+    s.meshes[0] = (v, i, tr, fi)
+    v, i, tr, _ = s.meshes[2]
+    s.meshes[2] = (v, i, tr, wi)
+    s.add_mesh(*S.box_mesh((0.35, 0.55, 0.25), (0.3, 0.3, 0.5), 20.0), bi)
+    s.add_mesh(*S.quad_mesh((0.6, 0.7, 0.05), (0.25, 0, 0), (0, 0, 0.25)), gi)
+    return s
+
+
 PIN_SCENES = {
     "cornell": cornell, "disney_ibl": disney_ibl, "lights_icosphere": lights_icosphere, "media": media,
     "transparent": transparent, "media_transparent": media_transparent, "ortho_sky": ortho_sky,
-    "thin_lens_reinhard": thin_lens_reinhard, "no_tonemap": no_tonemap,
+    "thin_lens_reinhard": thin_lens_reinhard, "no_tonemap": no_tonemap, "textured": textured,
 }

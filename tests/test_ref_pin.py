@@ -16,7 +16,7 @@ if not ref.available():
     pytest.skip("reference checkout not present", allow_module_level=True)
 
 
-@pytest.mark.parametrize("name", ["cornell", "media_transparent", "lights_icosphere"])
+@pytest.mark.parametrize("name", ["cornell", "media_transparent", "lights_icosphere", "textured"])
 def test_reference_shaders_match_oracle_over_more_frames(oracle_mod, name):
     sc = pin_scenes.PIN_SCENES[name]()
     frames = sc.spp + 3
