@@ -7,7 +7,7 @@
 `--workload` renders one of the procedural scenes; `-c` reads the reference's
 YAML schema (window, tracer, scene_file, hdri_*, colours). The window and
 interactive "Save" button of the reference become `--out`, which writes
-<PREFIX>_color.pfm, _albedo.pfm, _normal.pfm and _final.ppm.
+<PREFIX>_color.pfm, _albedo.pfm, _normal.pfm, _final.ppm and _final.png.
 """
 import argparse
 import importlib
@@ -19,6 +19,19 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
+
+
+def resolve(path, config_dir):
+    """A config path: as given (relative to the working directory, like the
+    reference binary run from its checkout), else next to the config file or
+    its parent directory."""
+    if os.path.isabs(path) or os.path.exists(path):
+        return path
+    for base in (config_dir, os.path.dirname(config_dir)):
+        p = os.path.join(base, path)
+        if os.path.exists(p):
+            return p
+    return path
 
 
 def main(argv=None):
@@ -37,17 +50,19 @@ def main(argv=None):
     if args.config:
         cfgmod = importlib.import_module("hala-pathtracer_gb300.config")
         cfg = cfgmod.load_app_config(args.config)
-        cfgmod.validate_app_config(cfg, base_dir=os.path.dirname(os.path.abspath(args.config)))
+        cfgmod.validate_app_config(cfg, check_scene_file=False)
         loader = importlib.import_module("hala-pathtracer_gb300.gltf")
         base = os.path.dirname(os.path.abspath(args.config))
-        scene = loader.load_scene(os.path.join(base, cfg.scene_file) if not os.path.isabs(cfg.scene_file)
-                                  else cfg.scene_file)
+        scene_path = resolve(cfg.scene_file, base)
+        if not os.path.exists(scene_path):
+            raise cfgmod.ConfigError(f'The scene file "{cfg.scene_file}" is not found.')
+        scene = loader.load_scene(scene_path, cfg.window.width, cfg.window.height)
         env = cfgmod.environment_settings(cfg)
         r = pt.Renderer(cfgmod.tracer_config(cfg, seed=args.seed or 0, wave_paths=args.wave))
         r.set_scene(scene)
         if env["hdri_file"]:
             exr = importlib.import_module("hala-pathtracer_gb300.exr")
-            r.set_envmap(exr.read_exr(os.path.join(base, env["hdri_file"])), env["hdri_rotation"])
+            r.set_envmap(exr.read_rgb(resolve(env["hdri_file"], base)), env["hdri_rotation"])
         else:
             r.set_ground_color(env["ground_color"])
             r.set_sky_color(env["sky_color"])
@@ -73,7 +88,9 @@ def main(argv=None):
           f"BVH build {st.bvh_build_ms:.2f} ms", flush=True)
     if args.out:
         r.save_images(args.out)
-        print(f"wrote {args.out}_color.pfm, _albedo.pfm, _normal.pfm, _final.ppm")
+        png = importlib.import_module("hala-pathtracer_gb300.png")
+        png.write(args.out + "_final.png", r.image(pt.abi.IMAGE_FINAL)[..., :3])
+        print(f"wrote {args.out}_color.pfm, _albedo.pfm, _normal.pfm, _final.ppm, _final.png")
     r.close()
     return 0
 
