@@ -364,7 +364,7 @@ def main():
     e2e_value = ws * paths_step * args.steps / (e2e_total / 1e3)
 
     # roofline of the closest-hit kernel (algorithmic bytes per traced ray)
-    bytes_per_ray = 32 + 16 + 64 * nodes_per_ray + 48 * tris_per_ray
+    bytes_per_ray = 32 + 16 + 128 * nodes_per_ray + 48 * tris_per_ray  # 128-B 4-wide nodes, 48-B triangles
     avg_launch_ms = trace_ms / max(trace_launches, 1)
     achieved = bytes_per_ray * closest / (trace_ms / 1e3) / 1e9 if trace_ms > 0 else 0.0
     peak, peak_kind = _peaks()

@@ -224,9 +224,10 @@ uint64_t renderer_estimate_bytes(const pt_scene_desc* d, uint32_t width, uint32_
   }
   const uint64_t V = std::max<uint64_t>(nv, 1), T = std::max<uint64_t>(nt, 1);
   // vertices: raw 44 + normal/tangent/position 48 + uv 8
-  // triangles: raw indices 12 + v0/e1/e2 48 + sorted 48 + 2 nodes 128 +
-  // vertex ids 12 + material 4; the BVH build's scratch is about 64 B more
-  uint64_t b = V * 100 + T * (252 + 64);
+  // triangles: raw indices 12 + v0/e1/e2 48 + sorted 48 + 4-wide nodes
+  // (capacity 2 per triangle) 256 + vertex ids 12 + material 4; the BVH
+  // build's scratch (binary nodes and queues) is about 190 B more
+  uint64_t b = V * 100 + T * (380 + 190);
   b += (uint64_t)d->num_materials * sizeof(pt_material) + 4096;
   for (uint32_t i = 0; i < d->num_textures; ++i) b += 16ull * d->textures[i].width * d->textures[i].height + 16;
   const uint64_t E = (uint64_t)env_w * env_h;
@@ -358,11 +359,18 @@ pt_status cache_prepare(pt_renderer* r, uint32_t cap) {
     if (cs != PT_OK) return fail(r, cs, "radiance cache creation failed");
     float lo[3] = {-1, -1, -1}, hi[3] = {1, 1, 1};
     if (r->nnodes > 0) {
-      float4 root[4];
+      // union of the root's child boxes (unused slots are +inf: skip them)
+      float4 root[6];
       CK(r, cudaMemcpy(root, r->nodes.p, sizeof(root), cudaMemcpyDeviceToHost));
-      float b[6] = {std::fmin(root[0].x, root[1].x), std::fmax(root[0].y, root[1].y),
-                    std::fmin(root[0].z, root[1].z), std::fmax(root[0].w, root[1].w),
-                    std::fmin(root[2].x, root[2].z), std::fmax(root[2].y, root[2].w)};
+      float b[6] = {INFINITY, -INFINITY, INFINITY, -INFINITY, INFINITY, -INFINITY};
+      for (int k = 0; k < 4; ++k) {
+        const float* q[6] = {&root[0].x, &root[1].x, &root[2].x, &root[3].x, &root[4].x, &root[5].x};
+        if (!(q[0][k] < INFINITY)) continue;
+        for (int a = 0; a < 3; ++a) {
+          b[2 * a] = std::fmin(b[2 * a], q[2 * a][k]);
+          b[2 * a + 1] = std::fmax(b[2 * a + 1], q[2 * a + 1][k]);
+        }
+      }
       for (int i = 0; i < 3; ++i) {
         float l = b[2 * i], h = b[2 * i + 1];
         if (!(h > l)) {
@@ -656,17 +664,25 @@ pt_status pt_renderer_commit(pt_renderer* r) {
   }
   r->features = f;
   cudaStream_t st = r->stream;
-  CK(r, r->nodes.ensure(4 * (size_t)std::max<uint32_t>(2 * r->ntris, 2)));
   CK(r, r->tri_sorted.ensure(3 * (size_t)std::max<uint32_t>(r->ntris, 1)));
   CK(r, cudaEventRecord(r->ev0, st));
   if (r->ntris > 0) {
-    BvhBuffers bb{r->nodes.p, r->tri_sorted.p, 2 * r->ntris};
-    uint32_t nn = 0;
+    // binary SAH tree first (scratch), then its 4-wide collapse for traversal
+    Buf<float4> bin;
+    const uint32_t cap = 2 * r->ntris;
+    CK(r, bin.ensure(4 * (size_t)cap));
+    BvhBuffers bb{bin.p, r->tri_sorted.p, cap};
+    uint32_t nn = 0, nn4 = 0;
     int rc = build_bvh(r->tri_v0.p, r->tri_e1.p, r->tri_e2.p, r->ntris, bb, &nn, st);
     if (rc == 2) return fail(r, PT_ERR_OOM, "BVH build: out of device memory");
     if (rc != 0) return fail(r, PT_ERR_CUDA, "BVH build failed (code " + std::to_string(rc) + ")");
-    r->nnodes = nn;
+    CK(r, r->nodes.ensure(8 * (size_t)std::max<uint32_t>(nn, 1)));
+    rc = collapse_bvh4(bin.p, nn, r->nodes.p, std::max<uint32_t>(nn, 1), &nn4, st);
+    if (rc == 2) return fail(r, PT_ERR_OOM, "BVH collapse: out of device memory");
+    if (rc != 0) return fail(r, PT_ERR_CUDA, "BVH collapse failed (code " + std::to_string(rc) + ")");
+    r->nnodes = nn4;
   } else {
+    CK(r, r->nodes.ensure(8));
     r->nnodes = 0;
   }
   CK(r, cudaEventRecord(r->ev1, st));

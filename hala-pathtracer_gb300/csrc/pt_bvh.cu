@@ -295,6 +295,95 @@ __global__ void k_reorder(const uint32_t* final_ids, uint32_t n, const float4* v
 
 // Build scratch from the stream-ordered allocator of the build stream: no
 // allocation or free here waits for work on other streams.
+// ---------------------------------------------------------------------------
+// Collapse of the binary BVH into the 4-wide traversal layout (pt_types.h):
+// each 4-wide node takes a binary node's two children and keeps replacing
+// its internal child of largest surface area by that child's two children
+// until it has four. One launch per level of the 4-wide tree.
+struct CollapseWork {
+  int32_t bin;  // binary node
+  int32_t out;  // its 4-wide node
+};
+
+__device__ __forceinline__ float bin_child_area(const float4* bin, int32_t node, int c) {
+  const float4* nd = bin + 4 * node;
+  float4 a = nd[c], z = nd[2];
+  float lz = c ? z.z : z.x, hz = c ? z.w : z.y;
+  return box_area(a.x, a.z, lz, a.y, a.w, hz);
+}
+
+__global__ void k_collapse(const float4* bin, const CollapseWork* work, uint32_t nwork, float4* out4,
+                           uint32_t* node_counter, uint32_t cap4, CollapseWork* next, uint32_t* next_count,
+                           uint32_t* overflow) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nwork) return;
+  const CollapseWork w = work[i];
+  float lo[4][3], hi[4][3], area[4];
+  int32_t link[4];
+  int n = 0;
+  // child c of binary node `node` into slot k
+  auto load = [&](int32_t node, int c, int k) {
+    const float4* nd = bin + 4 * node;
+    float4 a = nd[c], z = nd[2];
+    int4 l = *reinterpret_cast<const int4*>(nd + 3);
+    lo[k][0] = a.x;
+    hi[k][0] = a.y;
+    lo[k][1] = a.z;
+    hi[k][1] = a.w;
+    lo[k][2] = c ? z.z : z.x;
+    hi[k][2] = c ? z.w : z.y;
+    link[k] = c ? l.y : l.x;
+    area[k] = bin_child_area(bin, node, c);
+  };
+  load(w.bin, 0, 0);
+  load(w.bin, 1, 1);
+  n = 2;
+  while (n < 4) {
+    int best = -1;
+    float ba = -1.0f;
+    for (int k = 0; k < n; ++k)
+      if (link[k] >= 0 && area[k] > ba) {
+        ba = area[k];
+        best = k;
+      }
+    if (best < 0) break;
+    const int32_t node = link[best];
+    load(node, 1, n);     // second child appended (n < 4 here)
+    load(node, 0, best);  // first child replaces its parent
+    ++n;
+  }
+  float4* o = out4 + 8 * (size_t)w.out;
+  float q[6][4];
+  int32_t ol[4];
+  for (int k = 0; k < 4; ++k) {
+    if (k < n) {
+      for (int c = 0; c < 3; ++c) {
+        q[2 * c][k] = lo[k][c];
+        q[2 * c + 1][k] = hi[k][c];
+      }
+      int32_t l = link[k];
+      if (l >= 0) {
+        uint32_t slot = atomicAdd(node_counter, 1u);
+        if (slot >= cap4) {
+          atomicAdd(overflow, 1u);
+          l = EMPTY_LINK;
+        } else {
+          uint32_t qi = atomicAdd(next_count, 1u);
+          next[qi] = CollapseWork{l, (int32_t)slot};
+          l = (int32_t)slot;
+        }
+      }
+      ol[k] = l;
+    } else {
+      for (int c = 0; c < 6; ++c) q[c][k] = INFINITY;  // never intersected (see pt_types.h)
+      ol[k] = EMPTY_LINK;
+    }
+  }
+  for (int c = 0; c < 6; ++c) o[c] = make_float4(q[c][0], q[c][1], q[c][2], q[c][3]);
+  o[6] = make_float4(__int_as_float(ol[0]), __int_as_float(ol[1]), __int_as_float(ol[2]), __int_as_float(ol[3]));
+  o[7] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
 template <class T>
 struct Tmp {
   T* p = nullptr;
@@ -355,6 +444,39 @@ int build_bvh(const float4* tri_v0, const float4* tri_e1, const float4* tri_e2, 
   k_reorder<<<(n + 255) / 256, 256, 0, st>>>(final_ids.p, n, tri_v0, tri_e1, tri_e2, out.tri_sorted);
   if (cudaStreamSynchronize(st) != cudaSuccess) return 3;
   *num_nodes = nn;
+  return 0;
+}
+
+int collapse_bvh4(const float4* bin, uint32_t nn_bin, float4* out4, uint32_t cap4, uint32_t* num4, cudaStream_t st) {
+  if (nn_bin == 0 || cap4 == 0) return 2;
+  Tmp<CollapseWork> qa, qb;
+  Tmp<uint32_t> counters;  // [0] 4-wide nodes, [1] next queue A, [2] next queue B, [3] overflow
+  const uint32_t qcap = nn_bin + 1;
+  if (qa.alloc(qcap, st) || qb.alloc(qcap, st) || counters.alloc(4, st)) return 2;
+  CollapseWork root{0, 0};
+  uint32_t init[4] = {1, 0, 0, 0};
+  cudaMemcpyAsync(qa.p, &root, sizeof(root), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(counters.p, init, sizeof(init), cudaMemcpyHostToDevice, st);
+  uint32_t nwork = 1, host = 0;
+  CollapseWork* cur = qa.p;
+  CollapseWork* nxt = qb.p;
+  int slot = 1;
+  for (int level = 0; level < 200 && nwork > 0; ++level) {
+    cudaMemsetAsync(counters.p + slot, 0, sizeof(uint32_t), st);
+    k_collapse<<<(nwork + 255) / 256, 256, 0, st>>>(bin, cur, nwork, out4, counters.p, cap4, nxt, counters.p + slot,
+                                                   counters.p + 3);
+    cudaMemcpyAsync(&host, counters.p + slot, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return 3;
+    nwork = host;
+    std::swap(cur, nxt);
+    slot = slot == 1 ? 2 : 1;
+  }
+  if (nwork != 0) return 4;
+  uint32_t res[4];
+  cudaMemcpyAsync(res, counters.p, sizeof(res), cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return 3;
+  if (res[3] != 0) return 5;
+  *num4 = res[0];
   return 0;
 }
 

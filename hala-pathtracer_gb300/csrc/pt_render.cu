@@ -113,7 +113,7 @@ __global__ void k_camera_multi(PathState P, const WaveSegment* segs, uint32_t ns
 
 // ------------------------------------------------------------------ trace
 template <bool BRUTE, bool COUNT, bool MULTI>
-__global__ void __launch_bounds__(256) k_trace(const __grid_constant__ DevScene S0, PathState P, QueueSet Q) {
+__global__ void __launch_bounds__(256, 5) k_trace(const __grid_constant__ DevScene S0, PathState P, QueueSet Q) {
   const uint32_t n = *Q.in_count;
   TravCount tc;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(256) k_trace(const __grid_constant__ DevScene 
 // ------------------------------------------------------------------ shadow rays
 // inc/lighting.glsl:116-149 and :203-238 (visibility + radiance += T * Ld)
 template <bool BRUTE, bool MULTI>
-__global__ void __launch_bounds__(256) k_shadow(const __grid_constant__ DevScene S0, PathState P, QueueSet Q) {
+__global__ void __launch_bounds__(256, 5) k_shadow(const __grid_constant__ DevScene S0, PathState P, QueueSet Q) {
   const uint32_t n = Q.counts[Q_SHADOW];
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     uint32_t p = Q.shadow[i];

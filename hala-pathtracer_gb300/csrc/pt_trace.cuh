@@ -144,7 +144,41 @@ __device__ __forceinline__ float3 slab_inv(float3 d) {
   return make_float3(r(d.x), r(d.y), r(d.z));
 }
 
+// Slab test of the four children of a 4-wide node (same arithmetic as the
+// binary test, one lane per child).
+__device__ __forceinline__ void quad_slabs(const float4* nd, float3 o, float3 inv, float tmin, float tmax,
+                                           float (&tn)[4], bool (&hit)[4]) {
+  const float4 lx = __ldg(nd), hx = __ldg(nd + 1), ly = __ldg(nd + 2), hy = __ldg(nd + 3);
+  const float4 lz = __ldg(nd + 4), hz = __ldg(nd + 5);
+  const float ox = o.x * inv.x, oy = o.y * inv.y, oz = o.z * inv.z;
+  const float LX[4] = {lx.x, lx.y, lx.z, lx.w}, HX[4] = {hx.x, hx.y, hx.z, hx.w};
+  const float LY[4] = {ly.x, ly.y, ly.z, ly.w}, HY[4] = {hy.x, hy.y, hy.z, hy.w};
+  const float LZ[4] = {lz.x, lz.y, lz.z, lz.w}, HZ[4] = {hz.x, hz.y, hz.z, hz.w};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    float a0 = fmaf(LX[k], inv.x, -ox), b0 = fmaf(HX[k], inv.x, -ox);
+    float a1 = fmaf(LY[k], inv.y, -oy), b1 = fmaf(HY[k], inv.y, -oy);
+    float a2 = fmaf(LZ[k], inv.z, -oz), b2 = fmaf(HZ[k], inv.z, -oz);
+    float n = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), tmin));
+    float f = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), tmax));
+    tn[k] = n;
+    hit[k] = n <= f * 1.0000005f;
+  }
+}
+
+__device__ __forceinline__ void cswap(float& ka, int32_t& va, float& kb, int32_t& vb) {
+  if (kb < ka) {
+    float tk = ka;
+    ka = kb;
+    kb = tk;
+    int32_t tv = va;
+    va = vb;
+    vb = tv;
+  }
+}
+
 constexpr int TRAV_STACK = 64;
+constexpr int TRAV4_STACK = 96;  // up to three entries per level of the 4-wide tree
 // Upper bound on node visits of one traversal; a well-formed tree never
 // reaches it, a corrupt one ends the traversal instead of looping.
 constexpr uint32_t TRAV_MAX_VISITS = 1u << 22;
@@ -173,34 +207,47 @@ __device__ __forceinline__ HitRec trace_tris_closest(const DevScene& S, float3 o
     return h;
   }
   if (S.num_tris == 0) return h;
-  float3 inv = slab_inv(d);
-  int32_t stack[TRAV_STACK];
+  const float3 inv = slab_inv(d);
+  int32_t st_link[TRAV4_STACK];
+  float st_t[TRAV4_STACK];
   int sp = 0;
   int32_t cur = 0;  // root is always internal
   uint32_t visits = 0;
   for (;;) {
     while (cur >= 0) {
-      if (++visits > TRAV_MAX_VISITS) return h;
+      if (++visits > TRAV_MAX_VISITS || cur == EMPTY_LINK) return h;
       if (COUNT) tc->nodes++;
-      const float4* nd = S.nodes + 4 * cur;
-      float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2);
-      int4 n3 = __ldg(reinterpret_cast<const int4*>(nd + 3));
-      bool h0, h1;
-      float tn0, tn1;
-      child_slabs(n0, n1, n2, o, inv, tmin, h.t, h0, h1, tn0, tn1);
-      if (h0 && h1) {
-        int32_t nearc = n3.x, farc = n3.y;
-        if (tn1 < tn0) { nearc = n3.y; farc = n3.x; }
-        if (sp < TRAV_STACK) stack[sp++] = farc;
-        cur = nearc;
-      } else if (h0) {
-        cur = n3.x;
-      } else if (h1) {
-        cur = n3.y;
-      } else {
-        cur = sp > 0 ? stack[--sp] : 0x7FFFFFFF;
+      const float4* nd = S.nodes + 8 * (size_t)cur;
+      float tn[4];
+      bool hit[4];
+      quad_slabs(nd, o, inv, tmin, h.t, tn, hit);
+      const int4 l = __ldg(reinterpret_cast<const int4*>(nd + 6));
+      // nearest first: sort (distance, link) with misses at +inf
+      float k0 = hit[0] ? tn[0] : INF, k1 = hit[1] ? tn[1] : INF, k2 = hit[2] ? tn[2] : INF,
+            k3 = hit[3] ? tn[3] : INF;
+      int32_t v0 = l.x, v1 = l.y, v2 = l.z, v3 = l.w;
+      const int nh = (int)hit[0] + (int)hit[1] + (int)hit[2] + (int)hit[3];
+      cswap(k0, v0, k1, v1);
+      cswap(k2, v2, k3, v3);
+      cswap(k0, v0, k2, v2);
+      cswap(k1, v1, k3, v3);
+      cswap(k1, v1, k2, v2);
+      if (nh == 0) {
+        cur = 0x7FFFFFFF;
+        while (sp > 0) {
+          --sp;
+          if (st_t[sp] <= h.t * 1.0000005f) {
+            cur = st_link[sp];
+            break;
+          }
+        }
         if (cur == 0x7FFFFFFF) return h;
+        continue;
       }
+      if (nh >= 4 && sp < TRAV4_STACK) { st_link[sp] = v3; st_t[sp] = k3; ++sp; }
+      if (nh >= 3 && sp < TRAV4_STACK) { st_link[sp] = v2; st_t[sp] = k2; ++sp; }
+      if (nh >= 2 && sp < TRAV4_STACK) { st_link[sp] = v1; st_t[sp] = k1; ++sp; }
+      cur = v0;
     }
     // leaf
     uint32_t start = (uint32_t)cur & 0x03FFFFFFu, count = ((uint32_t)cur >> 26) & 0x1Fu;
@@ -213,8 +260,15 @@ __device__ __forceinline__ HitRec trace_tris_closest(const DevScene& S, float3 o
         h.t = t; h.u = u; h.v = v; h.id = id;
       }
     }
-    if (sp == 0) return h;
-    cur = stack[--sp];
+    cur = 0x7FFFFFFF;
+    while (sp > 0) {
+      --sp;
+      if (st_t[sp] <= h.t * 1.0000005f) {
+        cur = st_link[sp];
+        break;
+      }
+    }
+    if (cur == 0x7FFFFFFF) return h;
   }
 }
 
@@ -229,33 +283,32 @@ __device__ __forceinline__ bool trace_tris_any(const DevScene& S, float3 o, floa
     return false;
   }
   if (S.num_tris == 0) return false;
-  float3 inv = slab_inv(d);
-  int32_t stack[TRAV_STACK];
+  const float3 inv = slab_inv(d);
+  int32_t stack[TRAV4_STACK];
   int sp = 0;
   int32_t cur = 0;
   uint32_t visits = 0;
   for (;;) {
     while (cur >= 0) {
-      if (++visits > TRAV_MAX_VISITS) return false;
-      const float4* nd = S.nodes + 4 * cur;
-      float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2);
-      int4 n3 = __ldg(reinterpret_cast<const int4*>(nd + 3));
-      bool h0, h1;
-      float tn0, tn1;
-      child_slabs(n0, n1, n2, o, inv, tmin, tmax, h0, h1, tn0, tn1);
-      if (h0 && h1) {
-        int32_t nearc = n3.x, farc = n3.y;
-        if (tn1 < tn0) { nearc = n3.y; farc = n3.x; }
-        if (sp < TRAV_STACK) stack[sp++] = farc;
-        cur = nearc;
-      } else if (h0) {
-        cur = n3.x;
-      } else if (h1) {
-        cur = n3.y;
-      } else {
-        if (sp == 0) return false;
-        cur = stack[--sp];
+      if (++visits > TRAV_MAX_VISITS || cur == EMPTY_LINK) return false;
+      const float4* nd = S.nodes + 8 * (size_t)cur;
+      float tn[4];
+      bool hit[4];
+      quad_slabs(nd, o, inv, tmin, tmax, tn, hit);
+      const int4 l = __ldg(reinterpret_cast<const int4*>(nd + 6));
+      const int32_t L[4] = {l.x, l.y, l.z, l.w};
+      int32_t next = 0x7FFFFFFF;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (!hit[k]) continue;
+        if (next == 0x7FFFFFFF) next = L[k];
+        else if (sp < TRAV4_STACK) stack[sp++] = L[k];
       }
+      if (next == 0x7FFFFFFF) {
+        if (sp == 0) return false;
+        next = stack[--sp];
+      }
+      cur = next;
     }
     uint32_t start = (uint32_t)cur & 0x03FFFFFFu, count = ((uint32_t)cur >> 26) & 0x1Fu;
     for (uint32_t s = start; s < start + count; ++s) {

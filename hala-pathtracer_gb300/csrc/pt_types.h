@@ -48,6 +48,15 @@ struct DevCamera {  // inc/types.glsl:2-11
 // link >= 0: internal node index; link < 0: leaf, start = link & 0x03FFFFFF
 // (slot in tri[]), count = (link >> 26) & 0x1F. An empty child has an
 // inverted box so it never intersects.
+// 4-wide BVH node used by the traversal (128 B = 8 x 16 B):
+//   q[0..5] = lo.x, hi.x, lo.y, hi.y, lo.z, hi.z of the four children
+//   q[6]    = the four child links (as above; EMPTY_LINK for an unused slot,
+//             whose box is +inf on every bound so that no ray enters it:
+//             both slab distances of an axis are then +inf or -inf)
+//   q[7]    = unused
+// It is collapsed from the binary tree: halving the depth halves the chain
+// of dependent node fetches a ray waits on.
+constexpr int32_t EMPTY_LINK = 0x7FFFFFFF;
 constexpr int32_t LEAF_BIT = (int32_t)0x80000000u;
 constexpr int LEAF_MAX = 8;
 
