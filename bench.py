@@ -259,6 +259,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="resolution scale of the workload (profiling captures of a smaller case)")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving mix")
     ap.add_argument("--no-cache", action="store_true", help="skip the radiance-cache comparison")
     ap.add_argument("--serving-jobs", type=int, default=256)
@@ -269,6 +271,9 @@ def main():
     scenes = importlib.import_module("hala-pathtracer_gb300.scenes")
     fn, kw = WORKLOADS[args.workload]
     scene = getattr(scenes, fn)(**kw)
+    if args.scale != 1.0:
+        scene.width = max(1, int(round(scene.width * args.scale)))
+        scene.height = max(1, int(round(scene.height * args.scale)))
     workload = {"workload": args.workload, "width": scene.width, "height": scene.height, "spp": scene.spp,
                 "max_depth": scene.max_depth, "rr_depth": scene.rr_depth, "triangles": scene.num_triangles,
                 "paths_per_step": scene.width * scene.height * scene.spp}
