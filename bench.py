@@ -41,6 +41,9 @@ WORKLOADS = {
 }
 DEFAULT_WORKLOAD = "disney_grid_1080p_64spp"
 L2_FLUSH_BYTES = 256 << 20  # > 129 MB L2
+# DRAM bytes (read + write) per closest-hit ray of k_trace, from the ncu
+# capture in profiles/k_trace_disney_grid_480x270_bvh4.md (bounces 0 and 1).
+TRACE_DRAM_BYTES_PER_RAY = (349.191168e6 + 173.670912e6 + 287.307520e6 + 114.504448e6) / (8294400 + 5583360)
 
 
 def _dist():
@@ -382,7 +385,9 @@ def main():
         "e2e": {"value": e2e_value, "unit": "paths/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_total / args.steps},
         "roofline": {"kernel": "k_trace (closest hit)", "bound": "hbm", "achieved": achieved, "peak": peak,
-                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": TRACE_DRAM_BYTES_PER_RAY * closest / max(trace_launches, 1),
+                     "traffic_note": "ncu DRAM bytes per ray (480x270 capture, bounces 0-1) x rays per launch",
                      "bytes_per_ray": bytes_per_ray, "nodes_per_ray": nodes_per_ray, "tris_per_ray": tris_per_ray,
                      "avg_launch_ms": avg_launch_ms, "launches": trace_launches,
                      "trace_share_of_step": trace_ms / max(total_ms, 1e-9)},
