@@ -53,6 +53,24 @@ def _dist():
     return ws, rank, local
 
 
+def rank_seed(seed, rank):
+    """Per-rank RNG seed offset: every rank renders its own sample range of
+    the workload (independent units, no data-path collective)."""
+    return seed + rank * 100003
+
+
+def max_over_ranks(x, device="cuda"):
+    """The slowest rank's time (the job's time) when running under
+    torch.distributed; x itself on a single process."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def _peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -294,7 +312,7 @@ def main():
     abi = pt.abi
     pt.build()
 
-    scene.seed = scene.seed + rank * 100003  # distinct sample range per rank
+    scene.seed = rank_seed(scene.seed, rank)  # distinct sample range per rank
     r = pt.renderer_for(scene)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
@@ -335,11 +353,7 @@ def main():
         launches += st.kernel_launches
     barrier()
     clk = clocks.stop()
-    total_ms = sum(step_ms)
-    if ws > 1:
-        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(sum(step_ms))
     paths_step = scene.width * scene.height * scene.spp
     value = ws * paths_step * args.steps / (total_ms / 1e3)
     rays_per_s = ws * (closest + shadow) / (total_ms / 1e3)
@@ -364,11 +378,7 @@ def main():
         barrier()
         if k >= args.warmup:
             e2e_ms.append(1e3 * (time.perf_counter() - t0))
-    e2e_total = sum(e2e_ms)
-    if ws > 1:
-        t = torch.tensor([e2e_total], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_total = float(t.item())
+    e2e_total = max_over_ranks(sum(e2e_ms))
     e2e_value = ws * paths_step * args.steps / (e2e_total / 1e3)
 
     # roofline of the closest-hit kernel (algorithmic bytes per traced ray)
