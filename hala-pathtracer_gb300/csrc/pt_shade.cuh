@@ -451,7 +451,7 @@ __device__ __forceinline__ void apply_maps(const DevScene& S, pt_material& m, Su
 }
 
 template <int MAT, bool MEDIUM, bool TRANSPARENT, bool MULTI, bool CACHE = false, bool TEXTURED = false>
-__global__ void __launch_bounds__(256) k_shade(const __grid_constant__ DevScene S0, PathState P, QueueSet Q) {
+__global__ void __launch_bounds__(256, MEDIUM ? 4 : 3) k_shade(const __grid_constant__ DevScene S0, PathState P, QueueSet Q) {
   const int slot = MAT == PT_MATERIAL_DISNEY ? Q_DISNEY : Q_DIFFUSE;
   const uint32_t* qin = MAT == PT_MATERIAL_DISNEY ? Q.disney : Q.diffuse;
   const uint32_t n = Q.counts[slot];
