@@ -117,24 +117,6 @@ struct HitRec {
   uint32_t id;
 };
 
-__device__ __forceinline__ void child_slabs(const float4 n0, const float4 n1, const float4 n2, float3 o, float3 inv,
-                                            float tmin, float tmax, bool& h0, bool& h1, float& tn0, float& tn1) {
-  // ray-box slabs for both children; far distance widened by ~2 ulp
-  float ox = o.x * inv.x, oy = o.y * inv.y, oz = o.z * inv.z;
-  float a0 = fmaf(n0.x, inv.x, -ox), b0 = fmaf(n0.y, inv.x, -ox);
-  float a1 = fmaf(n0.z, inv.y, -oy), b1 = fmaf(n0.w, inv.y, -oy);
-  float a2 = fmaf(n2.x, inv.z, -oz), b2 = fmaf(n2.y, inv.z, -oz);
-  float c0 = fmaf(n1.x, inv.x, -ox), d0 = fmaf(n1.y, inv.x, -ox);
-  float c1 = fmaf(n1.z, inv.y, -oy), d1 = fmaf(n1.w, inv.y, -oy);
-  float c2 = fmaf(n2.z, inv.z, -oz), d2 = fmaf(n2.w, inv.z, -oz);
-  tn0 = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), tmin));
-  float tf0 = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), tmax));
-  tn1 = fmaxf(fmaxf(fminf(c0, d0), fminf(c1, d1)), fmaxf(fminf(c2, d2), tmin));
-  float tf1 = fminf(fminf(fmaxf(c0, d0), fmaxf(c1, d1)), fminf(fmaxf(c2, d2), tmax));
-  h0 = tn0 <= tf0 * 1.0000005f;
-  h1 = tn1 <= tf1 * 1.0000005f;
-}
-
 // Reciprocal direction for the slab test. A component that is exactly zero
 // is replaced by +-1e-20 so fmaf(lo, inv, -o * inv) never forms inf - inf
 // (which would be NaN and cull boxes the ray passes through). Only culling
@@ -144,23 +126,42 @@ __device__ __forceinline__ float3 slab_inv(float3 d) {
   return make_float3(r(d.x), r(d.y), r(d.z));
 }
 
-// Slab test of the four children of a 4-wide node (same arithmetic as the
-// binary test, one lane per child).
-__device__ __forceinline__ void quad_slabs(const float4* nd, float3 o, float3 inv, float tmin, float tmax,
+// Per-ray constants of the slab test: reciprocal direction, origin times it,
+// and which of each axis's two planes is the near one (the child boxes are
+// stored lo-then-hi per axis, so the near plane is entry 0 or 1).
+struct SlabRay {
+  float3 inv, oinv;
+  int nx, ny, nz;
+};
+__device__ __forceinline__ SlabRay slab_ray(float3 o, float3 d) {
+  SlabRay r;
+  r.inv = slab_inv(d);
+  r.oinv = make_float3(o.x * r.inv.x, o.y * r.inv.y, o.z * r.inv.z);
+  r.nx = r.inv.x < 0.0f ? 1 : 0;
+  r.ny = r.inv.y < 0.0f ? 1 : 0;
+  r.nz = r.inv.z < 0.0f ? 1 : 0;
+  return r;
+}
+
+// Slab test of the four children of a 4-wide node, one lane per child. The
+// near and far planes of each axis are picked by the ray's direction signs
+// when loading, which gives exactly min/max of the two plane distances (the
+// distance is monotonic in the plane coordinate, lo <= hi).
+__device__ __forceinline__ void quad_slabs(const float4* nd, const SlabRay& r, float tmin, float tmax,
                                            float (&tn)[4], bool (&hit)[4]) {
-  const float4 lx = __ldg(nd), hx = __ldg(nd + 1), ly = __ldg(nd + 2), hy = __ldg(nd + 3);
-  const float4 lz = __ldg(nd + 4), hz = __ldg(nd + 5);
-  const float ox = o.x * inv.x, oy = o.y * inv.y, oz = o.z * inv.z;
-  const float LX[4] = {lx.x, lx.y, lx.z, lx.w}, HX[4] = {hx.x, hx.y, hx.z, hx.w};
-  const float LY[4] = {ly.x, ly.y, ly.z, ly.w}, HY[4] = {hy.x, hy.y, hy.z, hy.w};
-  const float LZ[4] = {lz.x, lz.y, lz.z, lz.w}, HZ[4] = {hz.x, hz.y, hz.z, hz.w};
+  const float4 nx = __ldg(nd + r.nx), fx = __ldg(nd + 1 - r.nx);
+  const float4 ny = __ldg(nd + 2 + r.ny), fy = __ldg(nd + 3 - r.ny);
+  const float4 nz = __ldg(nd + 4 + r.nz), fz = __ldg(nd + 5 - r.nz);
+  const float NX[4] = {nx.x, nx.y, nx.z, nx.w}, FX[4] = {fx.x, fx.y, fx.z, fx.w};
+  const float NY[4] = {ny.x, ny.y, ny.z, ny.w}, FY[4] = {fy.x, fy.y, fy.z, fy.w};
+  const float NZ[4] = {nz.x, nz.y, nz.z, nz.w}, FZ[4] = {fz.x, fz.y, fz.z, fz.w};
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    float a0 = fmaf(LX[k], inv.x, -ox), b0 = fmaf(HX[k], inv.x, -ox);
-    float a1 = fmaf(LY[k], inv.y, -oy), b1 = fmaf(HY[k], inv.y, -oy);
-    float a2 = fmaf(LZ[k], inv.z, -oz), b2 = fmaf(HZ[k], inv.z, -oz);
-    float n = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), tmin));
-    float f = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), tmax));
+    float a0 = fmaf(NX[k], r.inv.x, -r.oinv.x), b0 = fmaf(FX[k], r.inv.x, -r.oinv.x);
+    float a1 = fmaf(NY[k], r.inv.y, -r.oinv.y), b1 = fmaf(FY[k], r.inv.y, -r.oinv.y);
+    float a2 = fmaf(NZ[k], r.inv.z, -r.oinv.z), b2 = fmaf(FZ[k], r.inv.z, -r.oinv.z);
+    float n = fmaxf(fmaxf(a0, a1), fmaxf(a2, tmin));
+    float f = fminf(fminf(b0, b1), fminf(b2, tmax));
     tn[k] = n;
     hit[k] = n <= f * 1.0000005f;
   }
@@ -207,7 +208,7 @@ __device__ __forceinline__ HitRec trace_tris_closest(const DevScene& S, float3 o
     return h;
   }
   if (S.num_tris == 0) return h;
-  const float3 inv = slab_inv(d);
+  const SlabRay sr = slab_ray(o, d);
   int32_t st_link[TRAV4_STACK];
   float st_t[TRAV4_STACK];
   int sp = 0;
@@ -220,7 +221,7 @@ __device__ __forceinline__ HitRec trace_tris_closest(const DevScene& S, float3 o
       const float4* nd = S.nodes + 8 * (size_t)cur;
       float tn[4];
       bool hit[4];
-      quad_slabs(nd, o, inv, tmin, h.t, tn, hit);
+      quad_slabs(nd, sr, tmin, h.t, tn, hit);
       const int4 l = __ldg(reinterpret_cast<const int4*>(nd + 6));
       // nearest first: sort (distance, link) with misses at +inf
       float k0 = hit[0] ? tn[0] : INF, k1 = hit[1] ? tn[1] : INF, k2 = hit[2] ? tn[2] : INF,
@@ -283,7 +284,7 @@ __device__ __forceinline__ bool trace_tris_any(const DevScene& S, float3 o, floa
     return false;
   }
   if (S.num_tris == 0) return false;
-  const float3 inv = slab_inv(d);
+  const SlabRay sr = slab_ray(o, d);
   int32_t stack[TRAV4_STACK];
   int sp = 0;
   int32_t cur = 0;
@@ -294,7 +295,7 @@ __device__ __forceinline__ bool trace_tris_any(const DevScene& S, float3 o, floa
       const float4* nd = S.nodes + 8 * (size_t)cur;
       float tn[4];
       bool hit[4];
-      quad_slabs(nd, o, inv, tmin, tmax, tn, hit);
+      quad_slabs(nd, sr, tmin, tmax, tn, hit);
       const int4 l = __ldg(reinterpret_cast<const int4*>(nd + 6));
       const int32_t L[4] = {l.x, l.y, l.z, l.w};
       int32_t next = 0x7FFFFFFF;
