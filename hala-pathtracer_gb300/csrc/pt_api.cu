@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -463,6 +464,25 @@ pt_status pt_renderer_create(const pt_tracer_config* cfg, pt_renderer** out) {
 
 }  // extern "C"
 
+namespace {
+// The stream-ordered allocator of each device keeps freed blocks for reuse
+// instead of returning them to the driver at every synchronisation, so
+// renderers created one after another (jobs of a serving loop, repeated
+// end-to-end renders) reuse the wavefront and scene buffers of the last one.
+void keep_pool_memory(int device) {
+  static std::mutex mu;
+  static std::vector<int> done;
+  std::lock_guard<std::mutex> g(mu);
+  if (std::find(done.begin(), done.end(), device) != done.end()) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  done.push_back(device);
+}
+}  // namespace
+
 pt_status hpt::renderer_create_with_priority(const pt_tracer_config* cfg, int priority, pt_renderer** out) {
   if (!cfg || !out) return PT_ERR_INVALID_ARG;
   *out = nullptr;
@@ -470,6 +490,9 @@ pt_status hpt::renderer_create_with_priority(const pt_tracer_config* cfg, int pr
   if (cs != PT_OK) return cs;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PT_ERR_CUDA;
+  int device = 0;
+  cudaGetDevice(&device);
+  keep_pool_memory(device);
   pt_renderer* r = new pt_renderer();
   r->cfg = *cfg;
   if (cudaStreamCreateWithPriority(&r->stream, cudaStreamNonBlocking, priority) != cudaSuccess ||
