@@ -6,10 +6,15 @@
 // (bin boxes kept as order-preserving integers in shared memory), picks the
 // cheapest SAH plane, and stably partitions the task's triangle ids into the
 // other ping-pong buffer with a block-wide scan. Leaves (<= 4 triangles, or
-// when SAH says so) copy their ids into the final order. A layout pass then
-// writes the 64-byte traversal nodes and the triangles in leaf order.
+// when SAH says so) copy their ids into the final order. Tasks of more than
+// LARGE_TASK triangles (the top levels of big scenes) are spread over many
+// blocks instead (k_large_*), with the same planes and the same partition
+// order. A layout pass then writes the 64-byte binary nodes and the
+// triangles in leaf order; k_collapse turns the binary tree into the 4-wide
+// traversal nodes.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <mutex>
 #include <vector>
@@ -73,11 +78,36 @@ __device__ __forceinline__ float warp_max(float v) {
   return v;
 }
 
+constexpr uint32_t MAX_LARGE_TASKS = 1024;  // capacity of the per-level large-task list
+
+// Appends the two children of a split task to the next level's task list,
+// or to the list of large tasks (count > large_min) that the multi-block
+// path handles.
+__device__ __forceinline__ void push_children(uint32_t c, const BuildTask& t, uint32_t nleft, BuildTask* next_tasks,
+                                              uint32_t* next_count, BuildTask* next_large,
+                                              uint32_t* next_large_count, uint32_t large_min) {
+  const BuildTask kids[2] = {BuildTask{c, t.start, nleft, 0}, BuildTask{c + 1, t.start + nleft, t.count - nleft, 0}};
+  for (int k = 0; k < 2; ++k) {
+    if (kids[k].count > large_min) {
+      const uint32_t q = atomicAdd(next_large_count, 1u);
+      if (q < MAX_LARGE_TASKS) {
+        next_large[q] = kids[k];
+        continue;
+      }
+      // the large list is full: the one-block path handles it (slower, same tree)
+    }
+    next_tasks[atomicAdd(next_count, 1u)] = kids[k];
+  }
+}
+
 __global__ void __launch_bounds__(BUILD_THREADS) k_level(const BuildTask* tasks, const uint32_t* ntasks_ptr,
                                                          const uint32_t* src, uint32_t* dst, uint32_t* final_ids,
                                                          const float4* tlo, const float4* thi, const float4* tc,
                                                          BuildNode* nodes, uint32_t* node_counter,
-                                                         BuildTask* next_tasks, uint32_t* next_count) {
+                                                         BuildTask* next_tasks, uint32_t* next_count,
+                                                         BuildTask* next_large = nullptr,
+                                                         uint32_t* next_large_count = nullptr,
+                                                         uint32_t large_min = 0xFFFFFFFFu) {
   __shared__ float red[12][BUILD_THREADS / 32];
   __shared__ float box[12];
   __shared__ int bcnt[3][NB];
@@ -252,9 +282,273 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_level(const BuildTask* tasks,
     nd.right = (int32_t)(c + 1);
     nd.start = 0;
     nd.count = 0;
-    uint32_t q = atomicAdd(next_count, 2u);
-    next_tasks[q] = BuildTask{c, t.start, nleft, 0};
-    next_tasks[q + 1] = BuildTask{c + 1, t.start + nleft, t.count - nleft, 0};
+    push_children(c, t, nleft, next_tasks, next_count, next_large, next_large_count, large_min);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Large tasks (the top levels of big scenes): one task would keep a single
+// block busy for millions of triangles while the rest of the GPU idles, so
+// tasks above LARGE_TASK triangles are split over blocks of CHUNK triangles:
+// bounds and bins are merged into per-task state with order-preserving
+// integer atomics, one thread per task picks the plane, and the stable
+// partition uses per-chunk left counts (each chunk sums the counts of the
+// chunks before it).
+constexpr uint32_t LARGE_TASK = 1u << 15;
+constexpr uint32_t CHUNK = 4096;
+constexpr uint32_t MAX_LARGE = MAX_LARGE_TASKS;
+
+struct LargeState {
+  int box[12];  // lo xyz, centroid lo xyz, hi xyz, centroid hi xyz (ordered ints)
+  int bcnt[3][NB];
+  int bmin[3][NB][3];
+  int bmax[3][NB][3];
+  int best;        // plane a * (NB - 1) + s, or -1 for a median split
+  uint32_t nleft;
+};
+
+// Block -> (large task, chunk) through the per-task first-chunk prefix.
+__device__ __forceinline__ uint32_t chunk_task(const uint32_t* first_chunk, uint32_t nlarge, uint32_t block) {
+  uint32_t lo = 0, hi = nlarge;
+  while (hi - lo > 1) {
+    uint32_t mid = (lo + hi) / 2;
+    if (first_chunk[mid] <= block) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+__global__ void k_large_init(LargeState* st, uint32_t nlarge) {
+  LargeState& S = st[blockIdx.x];
+  for (int k = threadIdx.x; k < 12; k += blockDim.x) S.box[k] = f2o(k < 6 ? 1e30f : -1e30f);
+  for (int k = threadIdx.x; k < 3 * NB; k += blockDim.x) {
+    int a = k / NB, b = k % NB;
+    S.bcnt[a][b] = 0;
+    for (int c = 0; c < 3; ++c) {
+      S.bmin[a][b][c] = f2o(1e30f);
+      S.bmax[a][b][c] = f2o(-1e30f);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(BUILD_THREADS) k_large_bounds(const BuildTask* large, const uint32_t* first_chunk,
+                                                                uint32_t nlarge, const uint32_t* src,
+                                                                const float4* tlo, const float4* thi,
+                                                                const float4* tc, LargeState* st) {
+  __shared__ float red[12][BUILD_THREADS / 32];
+  const uint32_t j = chunk_task(first_chunk, nlarge, blockIdx.x);
+  const BuildTask t = large[j];
+  const uint32_t b0 = t.start + (blockIdx.x - first_chunk[j]) * CHUNK;
+  const uint32_t b1 = min(t.start + t.count, b0 + CHUNK);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  float v[12];
+  for (int k = 0; k < 6; ++k) { v[k] = 1e30f; v[6 + k] = -1e30f; }
+  for (uint32_t i = b0 + tid; i < b1; i += BUILD_THREADS) {
+    uint32_t id = src[i];
+    float4 lo = tlo[id], hi = thi[id], c = tc[id];
+    v[0] = fminf(v[0], lo.x); v[1] = fminf(v[1], lo.y); v[2] = fminf(v[2], lo.z);
+    v[3] = fminf(v[3], c.x);  v[4] = fminf(v[4], c.y);  v[5] = fminf(v[5], c.z);
+    v[6] = fmaxf(v[6], hi.x); v[7] = fmaxf(v[7], hi.y); v[8] = fmaxf(v[8], hi.z);
+    v[9] = fmaxf(v[9], c.x);  v[10] = fmaxf(v[10], c.y); v[11] = fmaxf(v[11], c.z);
+  }
+  for (int k = 0; k < 6; ++k) { v[k] = warp_min(v[k]); v[6 + k] = warp_max(v[6 + k]); }
+  if (lane == 0)
+    for (int k = 0; k < 12; ++k) red[k][warp] = v[k];
+  __syncthreads();
+  if (tid < 12) {
+    float r = red[tid][0];
+    for (int w = 1; w < BUILD_THREADS / 32; ++w) r = tid < 6 ? fminf(r, red[tid][w]) : fmaxf(r, red[tid][w]);
+    if (tid < 6) atomicMin(&st[j].box[tid], f2o(r));
+    else atomicMax(&st[j].box[tid], f2o(r));
+  }
+}
+
+__global__ void __launch_bounds__(BUILD_THREADS) k_large_bin(const BuildTask* large, const uint32_t* first_chunk,
+                                                             uint32_t nlarge, const uint32_t* src,
+                                                             const float4* tlo, const float4* thi,
+                                                             const float4* tc, LargeState* st) {
+  __shared__ int bcnt[3][NB];
+  __shared__ int bmin[3][NB][3];
+  __shared__ int bmax[3][NB][3];
+  const uint32_t j = chunk_task(first_chunk, nlarge, blockIdx.x);
+  const BuildTask t = large[j];
+  const uint32_t b0 = t.start + (blockIdx.x - first_chunk[j]) * CHUNK;
+  const uint32_t b1 = min(t.start + t.count, b0 + CHUNK);
+  const int tid = threadIdx.x;
+  float clo[3], cext[3];
+  for (int a = 0; a < 3; ++a) {
+    clo[a] = o2f(st[j].box[3 + a]);
+    cext[a] = o2f(st[j].box[9 + a]) - clo[a];
+  }
+  for (int k = tid; k < 3 * NB; k += BUILD_THREADS) {
+    int a = k / NB, b = k % NB;
+    bcnt[a][b] = 0;
+    for (int c = 0; c < 3; ++c) { bmin[a][b][c] = f2o(1e30f); bmax[a][b][c] = f2o(-1e30f); }
+  }
+  __syncthreads();
+  for (uint32_t i = b0 + tid; i < b1; i += BUILD_THREADS) {
+    uint32_t id = src[i];
+    float4 c = tc[id], lo = tlo[id], hi = thi[id];
+    const float cc[3] = {c.x, c.y, c.z};
+    const int ilo[3] = {f2o(lo.x), f2o(lo.y), f2o(lo.z)};
+    const int ihi[3] = {f2o(hi.x), f2o(hi.y), f2o(hi.z)};
+    for (int a = 0; a < 3; ++a) {
+      if (!(cext[a] > 0.0f)) continue;
+      int b = min(NB - 1, max(0, (int)((cc[a] - clo[a]) * ((float)NB / cext[a]))));
+      atomicAdd(&bcnt[a][b], 1);
+      for (int k = 0; k < 3; ++k) {
+        atomicMin(&bmin[a][b][k], ilo[k]);
+        atomicMax(&bmax[a][b][k], ihi[k]);
+      }
+    }
+  }
+  __syncthreads();
+  for (int k = tid; k < 3 * NB; k += BUILD_THREADS) {
+    int a = k / NB, b = k % NB;
+    if (bcnt[a][b] == 0) continue;
+    atomicAdd(&st[j].bcnt[a][b], bcnt[a][b]);
+    for (int c = 0; c < 3; ++c) {
+      atomicMin(&st[j].bmin[a][b][c], bmin[a][b][c]);
+      atomicMax(&st[j].bmax[a][b][c], bmax[a][b][c]);
+    }
+  }
+}
+
+// One thread per large task: SAH over the merged bins (the same cost as
+// k_level), node box, children.
+__global__ void k_large_split(const BuildTask* large, uint32_t nlarge, LargeState* st, BuildNode* nodes,
+                              uint32_t* node_counter, BuildTask* next_tasks, uint32_t* next_count,
+                              BuildTask* next_large, uint32_t* next_large_count, uint32_t large_min) {
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nlarge) return;
+  const BuildTask t = large[j];
+  LargeState& S = st[j];
+  float box[12];
+  for (int k = 0; k < 12; ++k) box[k] = o2f(S.box[k]);
+  BuildNode& nd = nodes[t.node];
+  nd.lo[0] = box[0]; nd.lo[1] = box[1]; nd.lo[2] = box[2];
+  nd.hi[0] = box[6]; nd.hi[1] = box[7]; nd.hi[2] = box[8];
+  int bi = -1;
+  float bc = 3.0e38f;
+  for (int a = 0; a < 3; ++a) {
+    if (!(box[9 + a] - box[3 + a] > 0.0f)) continue;
+    for (int s = 0; s < NB - 1; ++s) {
+      float l[6] = {1e30f, 1e30f, 1e30f, -1e30f, -1e30f, -1e30f}, r[6] = {1e30f, 1e30f, 1e30f, -1e30f, -1e30f, -1e30f};
+      int nl = 0, nr = 0;
+      for (int b = 0; b < NB; ++b) {
+        float* dstb = b <= s ? l : r;
+        int cnt = S.bcnt[a][b];
+        if (cnt == 0) continue;
+        if (b <= s) nl += cnt; else nr += cnt;
+        for (int k = 0; k < 3; ++k) {
+          dstb[k] = fminf(dstb[k], o2f(S.bmin[a][b][k]));
+          dstb[3 + k] = fmaxf(dstb[3 + k], o2f(S.bmax[a][b][k]));
+        }
+      }
+      if (nl > 0 && nr > 0) {
+        float cost = box_area(l[0], l[1], l[2], l[3], l[4], l[5]) * nl + box_area(r[0], r[1], r[2], r[3], r[4], r[5]) * nr;
+        if (cost < bc) { bc = cost; bi = a * (NB - 1) + s; }
+      }
+    }
+  }
+  uint32_t nleft = t.count / 2;  // median split when no plane separates the centroids
+  if (bi >= 0) {
+    const int a = bi / (NB - 1), s = bi % (NB - 1);
+    nleft = 0;
+    for (int b = 0; b <= s; ++b) nleft += (uint32_t)S.bcnt[a][b];
+  }
+  S.best = bi;
+  S.nleft = nleft;
+  uint32_t c = atomicAdd(node_counter, 2u);
+  nd.left = (int32_t)c;
+  nd.right = (int32_t)(c + 1);
+  nd.start = 0;
+  nd.count = 0;
+  push_children(c, t, nleft, next_tasks, next_count, next_large, next_large_count, large_min);
+}
+
+__device__ __forceinline__ bool large_goes_left(const LargeState& S, float4 c, int a, int s) {
+  const float clo = o2f(S.box[3 + a]);
+  const float cext = o2f(S.box[9 + a]) - clo;
+  const float cc = a == 0 ? c.x : (a == 1 ? c.y : c.z);
+  const int b = min(NB - 1, max(0, (int)((cc - clo) * ((float)NB / cext))));
+  return b <= s;
+}
+
+__global__ void __launch_bounds__(BUILD_THREADS) k_large_count(const BuildTask* large, const uint32_t* first_chunk,
+                                                               uint32_t nlarge, const uint32_t* src,
+                                                               const float4* tc, const LargeState* st,
+                                                               uint32_t* chunk_left) {
+  __shared__ uint32_t wsum[BUILD_THREADS / 32];
+  const uint32_t j = chunk_task(first_chunk, nlarge, blockIdx.x);
+  const BuildTask t = large[j];
+  const LargeState& S = st[j];
+  const uint32_t b0 = t.start + (blockIdx.x - first_chunk[j]) * CHUNK;
+  const uint32_t b1 = min(t.start + t.count, b0 + CHUNK);
+  uint32_t n = 0;
+  if (S.best >= 0) {
+    const int a = S.best / (NB - 1), s = S.best % (NB - 1);
+    for (uint32_t i = b0 + threadIdx.x; i < b1; i += BUILD_THREADS) n += large_goes_left(S, tc[src[i]], a, s);
+  } else {
+    // median split: the first nleft positions of the task go left
+    for (uint32_t i = b0 + threadIdx.x; i < b1; i += BUILD_THREADS) n += (i - t.start) < S.nleft;
+  }
+  for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = n;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t tot = 0;
+    for (int w = 0; w < BUILD_THREADS / 32; ++w) tot += wsum[w];
+    chunk_left[blockIdx.x] = tot;
+  }
+}
+
+__global__ void __launch_bounds__(BUILD_THREADS) k_large_scatter(const BuildTask* large, const uint32_t* first_chunk,
+                                                                 uint32_t nlarge, const uint32_t* src, uint32_t* dst,
+                                                                 const float4* tc, const LargeState* st,
+                                                                 const uint32_t* chunk_left) {
+  __shared__ uint32_t wcount[BUILD_THREADS / 32];
+  __shared__ uint32_t base_s;
+  const uint32_t j = chunk_task(first_chunk, nlarge, blockIdx.x);
+  const BuildTask t = large[j];
+  const LargeState& S = st[j];
+  const uint32_t b0 = t.start + (blockIdx.x - first_chunk[j]) * CHUNK;
+  const uint32_t b1 = min(t.start + t.count, b0 + CHUNK);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) {
+    uint32_t l = 0;
+    for (uint32_t c = first_chunk[j]; c < blockIdx.x; ++c) l += chunk_left[c];
+    base_s = l;
+  }
+  __syncthreads();
+  uint32_t lbase = base_s;                    // left elements before this position
+  uint32_t rbase = (b0 - t.start) - base_s;   // right elements before this position
+  const int a = S.best >= 0 ? S.best / (NB - 1) : 0, s = S.best >= 0 ? S.best % (NB - 1) : 0;
+  for (uint32_t base = b0; base < b1; base += BUILD_THREADS) {
+    const uint32_t i = base + tid;
+    const bool valid = i < b1;
+    const uint32_t id = valid ? src[i] : 0u;
+    bool left = false;
+    if (valid) left = S.best >= 0 ? large_goes_left(S, tc[id], a, s) : (i - t.start) < S.nleft;
+    const unsigned m = __ballot_sync(0xffffffffu, left);
+    const unsigned mv = __ballot_sync(0xffffffffu, valid);
+    if (lane == 0) wcount[warp] = __popc(m);
+    __syncthreads();
+    uint32_t wl = 0, total_l = 0;
+    for (int w = 0; w < BUILD_THREADS / 32; ++w) {
+      if (w < warp) wl += wcount[w];
+      total_l += wcount[w];
+    }
+    const uint32_t chunk = min((uint32_t)BUILD_THREADS, b1 - base);
+    const uint32_t rank_l = wl + __popc(m & ((1u << lane) - 1u));
+    const uint32_t before = (uint32_t)(warp * 32) + __popc(mv & ((1u << lane) - 1u));
+    if (valid) {
+      if (left) dst[t.start + lbase + rank_l] = id;
+      else dst[t.start + S.nleft + rbase + (before - rank_l)] = id;
+    }
+    lbase += total_l;
+    rbase += chunk - total_l;
+    __syncthreads();
   }
 }
 
@@ -403,39 +697,75 @@ int build_bvh(const float4* tri_v0, const float4* tri_e1, const float4* tri_e2, 
               uint32_t* num_nodes, cudaStream_t st) {
   if (n == 0) return 0;
   Tmp<float4> tlo, thi, tc;
-  Tmp<uint32_t> ids_a, ids_b, final_ids, counters;
-  Tmp<BuildTask> tasks_a, tasks_b;
+  Tmp<uint32_t> ids_a, ids_b, final_ids, counters, first_chunk, chunk_left;
+  Tmp<BuildTask> tasks_a, tasks_b, large_a, large_b;
   Tmp<BuildNode> nodes;
+  Tmp<LargeState> lstate;
   const uint32_t cap = 2 * n;
+  const uint32_t max_chunks = n / CHUNK + MAX_LARGE + 1;
   if (tlo.alloc(n, st) || thi.alloc(n, st) || tc.alloc(n, st) || ids_a.alloc(n, st) || ids_b.alloc(n, st) ||
-      final_ids.alloc(n, st) || counters.alloc(4, st) || tasks_a.alloc(n + 1, st) || tasks_b.alloc(n + 1, st) ||
-      nodes.alloc(cap, st))
+      final_ids.alloc(n, st) || counters.alloc(8, st) || tasks_a.alloc(n + 1, st) || tasks_b.alloc(n + 1, st) ||
+      nodes.alloc(cap, st) || large_a.alloc(MAX_LARGE, st) || large_b.alloc(MAX_LARGE, st) ||
+      lstate.alloc(MAX_LARGE, st) || first_chunk.alloc(MAX_LARGE + 1, st) || chunk_left.alloc(max_chunks, st))
     return 2;
   k_prep<<<(n + 255) / 256, 256, 0, st>>>(tri_v0, tri_e1, tri_e2, n, tlo.p, thi.p, tc.p, ids_a.p);
-  // counters: [0] node counter, [1] task count A, [2] task count B
-  BuildTask root{0, 0, n, 0};
-  uint32_t init[4] = {1, 1, 0, 0};
-  cudaMemcpyAsync(tasks_a.p, &root, sizeof(root), cudaMemcpyHostToDevice, st);
+  // counters: [0] node counter, [1]/[2] small-task counts A/B, [3]/[4] large-task counts A/B
+  const BuildTask root{0, 0, n, 0};
+  const bool root_large = n > LARGE_TASK;
+  uint32_t init[8] = {1, root_large ? 0u : 1u, 0, root_large ? 1u : 0u, 0, 0, 0, 0};
+  cudaMemcpyAsync(root_large ? large_a.p : tasks_a.p, &root, sizeof(root), cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(counters.p, init, sizeof(init), cudaMemcpyHostToDevice, st);
-  uint32_t ntasks = 1;
+  uint32_t ntasks = root_large ? 0 : 1, nlarge = root_large ? 1 : 0;
+  std::vector<BuildTask> hlarge(MAX_LARGE);
+  hlarge[0] = root;
+  std::vector<uint32_t> hfirst(MAX_LARGE + 1);
   BuildTask* cur = tasks_a.p;
   BuildTask* nxt = tasks_b.p;
+  BuildTask* lcur = large_a.p;
+  BuildTask* lnxt = large_b.p;
   uint32_t* src = ids_a.p;
   uint32_t* dst = ids_b.p;
   int cur_slot = 1, nxt_slot = 2;
-  uint32_t host_count = 0;
-  for (int level = 0; level < 200 && ntasks > 0; ++level) {
+  uint32_t host_counts[8];
+  for (int level = 0; level < 200 && (ntasks > 0 || nlarge > 0); ++level) {
     cudaMemsetAsync(counters.p + nxt_slot, 0, sizeof(uint32_t), st);
-    k_level<<<ntasks, BUILD_THREADS, 0, st>>>(cur, counters.p + cur_slot, src, dst, final_ids.p, tlo.p, thi.p, tc.p,
-                                              nodes.p, counters.p, nxt, counters.p + nxt_slot);
-    cudaMemcpyAsync(&host_count, counters.p + nxt_slot, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    cudaMemsetAsync(counters.p + nxt_slot + 2, 0, sizeof(uint32_t), st);
+    if (ntasks > 0)
+      k_level<<<ntasks, BUILD_THREADS, 0, st>>>(cur, counters.p + cur_slot, src, dst, final_ids.p, tlo.p, thi.p,
+                                                tc.p, nodes.p, counters.p, nxt, counters.p + nxt_slot, lnxt,
+                                                counters.p + nxt_slot + 2, LARGE_TASK);
+    if (nlarge > 0) {
+      uint32_t nchunks = 0;
+      for (uint32_t j = 0; j < nlarge; ++j) {
+        hfirst[j] = nchunks;
+        nchunks += (hlarge[j].count + CHUNK - 1) / CHUNK;
+      }
+      hfirst[nlarge] = nchunks;
+      if (nchunks > max_chunks) return 6;
+      cudaMemcpyAsync(first_chunk.p, hfirst.data(), (nlarge + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+      k_large_init<<<nlarge, 64, 0, st>>>(lstate.p, nlarge);
+      k_large_bounds<<<nchunks, BUILD_THREADS, 0, st>>>(lcur, first_chunk.p, nlarge, src, tlo.p, thi.p, tc.p,
+                                                        lstate.p);
+      k_large_bin<<<nchunks, BUILD_THREADS, 0, st>>>(lcur, first_chunk.p, nlarge, src, tlo.p, thi.p, tc.p, lstate.p);
+      k_large_split<<<(nlarge + 63) / 64, 64, 0, st>>>(lcur, nlarge, lstate.p, nodes.p, counters.p, nxt,
+                                                       counters.p + nxt_slot, lnxt, counters.p + nxt_slot + 2,
+                                                       LARGE_TASK);
+      k_large_count<<<nchunks, BUILD_THREADS, 0, st>>>(lcur, first_chunk.p, nlarge, src, tc.p, lstate.p,
+                                                       chunk_left.p);
+      k_large_scatter<<<nchunks, BUILD_THREADS, 0, st>>>(lcur, first_chunk.p, nlarge, src, dst, tc.p, lstate.p,
+                                                         chunk_left.p);
+    }
+    cudaMemcpyAsync(host_counts, counters.p, sizeof(host_counts), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(hlarge.data(), lnxt, MAX_LARGE * sizeof(BuildTask), cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return 3;
-    ntasks = host_count;
+    ntasks = host_counts[nxt_slot];
+    nlarge = std::min(host_counts[nxt_slot + 2], MAX_LARGE);
     std::swap(cur, nxt);
+    std::swap(lcur, lnxt);
     std::swap(src, dst);
     std::swap(cur_slot, nxt_slot);
   }
-  if (ntasks != 0) return 4;
+  if (ntasks != 0 || nlarge != 0) return 4;
   uint32_t nn = 0;
   cudaMemcpyAsync(&nn, counters.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return 3;
