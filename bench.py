@@ -128,7 +128,7 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_baseline(scene, seconds=12.0, threads=0):
+def cpu_baseline(scene, seconds=12.0, threads=0, npix=None):
     """The oracle (CPU restatement of the reference integrator) on the host
     cores over a bounded, seeded sample of the workload: a fixed set of
     pixels rendered frame after frame (same RNG stream as the GPU) until
@@ -139,7 +139,7 @@ def cpu_baseline(scene, seconds=12.0, threads=0):
     o = oracle.Oracle(scene)
     WH = scene.width * scene.height
     rng = np.random.default_rng(1234)
-    npix = min(WH, 640 << 10)
+    npix = min(WH, npix or (640 << 10))
     pix = np.sort(rng.choice(WH, size=npix, replace=False)).astype(np.uint32)
     o.trace_paths(pix[:1024], 0, 1, threads)  # thread start-up, caches
     frames, dt = 0, 0.0
@@ -149,7 +149,13 @@ def cpu_baseline(scene, seconds=12.0, threads=0):
         frames += 1
         dt = time.perf_counter() - t0
     cores = threads if threads > 0 else (os.cpu_count() or 1)
+    # one core, for the per-core rate (a short sample of the same pixels)
+    t1 = time.perf_counter()
+    one = pix[:max(1, min(npix, 4096))]
+    o.trace_paths(one, 0, 1, 1)
+    single = len(one) / (time.perf_counter() - t1)
     return {"value": npix * frames / dt, "unit": "paths/s", "cores": cores, "kind": "port",
+            "single_thread_paths_per_s": single,
             "sample": f"{npix} seeded random pixels x {frames} spp of the full workload ({dt:.1f} s)"}
 
 
@@ -175,6 +181,66 @@ def run_reference(args, scene, workload):
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def workloads_leg(pt):
+    """The other configurations of the benchmark, each at its full size: the
+    Cornell box (also on the host cores, in full), the 2.6M-triangle
+    displaced icosphere (with its BVH rebuilt before every frame) and the
+    media box."""
+    scenes = importlib.import_module("hala-pathtracer_gb300.scenes")
+    out = {}
+    for name, fn in (("cornell_256_16spp", scenes.cornell), ("displaced_icosphere_1080p_32spp",
+                                                               scenes.displaced_icosphere),
+                     ("media_box_1024_128spp", scenes.media_box)):
+        s = fn()
+        r = pt.renderer_for(s)
+        r.render(min(2, s.spp))
+        r.reset()
+        r.render(s.spp)
+        st = r.stats()
+        row = {"paths": st.paths, "render_ms": st.render_ms, "paths_per_s": st.paths / (st.render_ms / 1e3),
+               "rays_per_s": (st.closest_rays + st.shadow_rays) / (st.render_ms / 1e3), "triangles": s.num_triangles,
+               "bvh_build_ms": st.bvh_build_ms}
+        if name.startswith("displaced"):
+            # BVH rebuilt and timed per frame
+            r.reset()
+            total = 0.0
+            for _ in range(s.spp):
+                r.commit()
+                total += r.stats().bvh_build_ms
+                r.render(1)
+                total += r.stats().render_ms
+            row["per_frame_rebuild"] = {"paths_per_s": st.paths / (total / 1e3), "ms_total": total}
+        r.close()
+        if name.startswith("cornell"):
+            row["cpu_oracle"] = cpu_baseline(s, seconds=30.0, npix=s.width * s.height)
+        out[name] = row
+    return out
+
+
+def cache_mlp_roofline():
+    """Device-timed radiance-cache kernels on 2^22 seeded records against the
+    measured bf16 tensor peak: 43,008 MLP FLOPs per query (2 x 21,504
+    weights), three times that per training sample (forward, input and
+    weight gradients)."""
+    cache = importlib.import_module("hala-pathtracer_gb300.cache")
+    c = cache.RadianceCache()
+    n = 1 << 22
+    infer_ms, train_ms = c.benchmark(n, 5)
+    c.close()
+    flops = 2.0 * 21504
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak, kind = float(json.load(f)["bf16_tflops"]), "measured"
+    except Exception:
+        peak, kind = 1900.0, "fallback"
+    inf_tf = flops * n / (infer_ms / 1e3) / 1e12
+    trn_tf = 3.0 * flops * n / (train_ms / 1e3) / 1e12
+    return {"kernel": "k_cache_infer (hash grid + 6-layer BF16 MLP, mma.sync)", "bound": "tensor",
+            "queries": n, "infer_ms": infer_ms, "queries_per_s": n / (infer_ms / 1e3), "achieved": inf_tf,
+            "peak": peak, "peak_kind": kind, "unit": "TFLOP/s", "frac": inf_tf / peak,
+            "train_ms_per_pass": train_ms, "train_tflops": trn_tf, "train_frac": trn_tf / peak}
 
 
 def cache_curves(pt, scene, ref, chunks, cache_options=None):
@@ -284,6 +350,7 @@ def main():
                     help="resolution scale of the workload (profiling captures of a smaller case)")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving mix")
     ap.add_argument("--no-cache", action="store_true", help="skip the radiance-cache comparison")
+    ap.add_argument("--no-workloads", action="store_true", help="skip the other workloads' table")
     ap.add_argument("--serving-jobs", type=int, default=256)
     args = ap.parse_args()
     if args.warmup < 3:
@@ -410,7 +477,16 @@ def main():
         except Exception as e:  # the checker is optional for the GPU number
             line["cpu_baseline"] = {"error": str(e)}
     r.close()
+    if rank == 0 and ws == 1 and not args.no_workloads:
+        try:
+            line["workloads"] = workloads_leg(pt)
+        except Exception as e:
+            line["workloads"] = {"error": f"{type(e).__name__}: {e}"}
     if rank == 0 and ws == 1 and not args.no_cache:
+        try:
+            line["cache_mlp_roofline"] = cache_mlp_roofline()
+        except Exception as e:
+            line["cache_mlp_roofline"] = {"error": f"{type(e).__name__}: {e}"}
         try:
             line["radiance_cache"] = radiance_cache_leg(pt)
         except Exception as e:

@@ -224,6 +224,8 @@ RENDERER_SIGNATURES = {
                                      C.c_void_p, C.POINTER(C.c_float)]),
     "pt_cache_train": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
                                  C.POINTER(C.c_float)]),
+    "pt_cache_benchmark": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double)]),
     "pt_renderer_set_radiance_cache": (C.c_int, [C.c_void_p, C.POINTER(CacheConfig)]),
     "pt_material_preprocess": (None, [C.POINTER(Material)]),
     "pt_material_default": (None, [C.POINTER(Material)]),

@@ -79,3 +79,9 @@ class RadianceCache:
         self._check(self._lib.pt_cache_train(self._h, r.ctypes.data, t.ctypes.data, len(r), int(steps),
                                              C.byref(loss)))
         return loss.value
+
+    def benchmark(self, n=1 << 22, iterations=10):
+        """Device ms of one inference and one training pass over n seeded records."""
+        a, b = C.c_double(), C.c_double()
+        self._check(self._lib.pt_cache_benchmark(self._h, int(n), int(iterations), C.byref(a), C.byref(b)))
+        return a.value, b.value

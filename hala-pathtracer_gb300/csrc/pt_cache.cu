@@ -619,6 +619,19 @@ __global__ void k_cache_init_grid(float* w, uint64_t count, uint64_t seed, float
   if (i < count) w[i] = scale * init_uniform(seed, i);
 }
 
+// Seeded query records inside the unit box (for the device-timed benchmark).
+__global__ void k_cache_bench_records(float4* rec, float4* tgt, uint32_t n, uint64_t seed) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float u[16];
+  for (int k = 0; k < 16; ++k) u[k] = 0.5f + 0.5f * init_uniform(seed, 16ull * i + k);
+  rec[4 * (size_t)i] = make_float4(u[0], u[1], u[2], u[3] * 2.0f - 1.0f);
+  rec[4 * (size_t)i + 1] = make_float4(u[4] * 2.0f - 1.0f, u[5] * 2.0f - 1.0f, u[6] * 2.0f - 1.0f, u[7] * 2.0f - 1.0f);
+  rec[4 * (size_t)i + 2] = make_float4(u[8] * 2.0f - 1.0f, u[9], u[10], u[11]);
+  rec[4 * (size_t)i + 3] = make_float4(u[12], u[13], u[14], 0.0f);
+  tgt[i] = make_float4(u[0] + u[9], u[1] + u[10], u[2] + u[11], 0.0f);
+}
+
 constexpr size_t SMEM_INFER = (size_t)(SMEM_WN + INFER_WARPS * TILE) * 2;
 constexpr size_t SMEM_TRAIN = (size_t)(SMEM_WN + SMEM_WK + CACHE_WARPS * TILE) * 2;
 constexpr uint32_t DW_ROWS_PER_BLOCK = 512;
@@ -977,6 +990,52 @@ pt_status pt_cache_gradients(pt_cache* c, const float* records, const float* tar
   if (loss) CCK(c, cudaMemcpyAsync(loss, c->loss.p, sizeof(float), cudaMemcpyDeviceToHost, st));
   CCK(c, cudaMemsetAsync(c->ggrad.p, 0, c->grid_count * sizeof(float), st));
   CCK(c, cudaStreamSynchronize(st));
+  return PT_OK;
+}
+
+
+pt_status pt_cache_benchmark(pt_cache* c, uint32_t n, uint32_t iterations, double* infer_ms, double* train_ms) {
+  if (!c || n == 0 || iterations == 0) return PT_ERR_INVALID_ARG;
+  cudaStream_t st = c->stream;
+  Buf<float4> rec, tgt, out;
+  CCK(c, rec.ensure(4 * (size_t)n));
+  CCK(c, tgt.ensure(n));
+  CCK(c, out.ensure(n));
+  k_cache_bench_records<<<(n + 255) / 256, 256, 0, st>>>(rec.p, tgt.p, n, 0x5EEDull);
+  cudaEvent_t e0, e1;
+  CCK(c, cudaEventCreate(&e0));
+  CCK(c, cudaEventCreate(&e1));
+  // warm-up, then timed inference
+  launch_cache_infer(c->V, rec.p, nullptr, nullptr, n, out.p, nullptr, st);
+  CCK(c, cudaEventRecord(e0, st));
+  for (uint32_t k = 0; k < iterations; ++k) launch_cache_infer(c->V, rec.p, nullptr, nullptr, n, out.p, nullptr, st);
+  CCK(c, cudaEventRecord(e1, st));
+  CCK(c, cudaEventSynchronize(e1));
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  if (infer_ms) *infer_ms = ms / iterations;
+  // training steps over the same samples (one pass of batch_size batches each)
+  const uint32_t keep = c->cfg.steps_per_pass;
+  c->cfg.steps_per_pass = 0;
+  uint32_t steps = 0;
+  CCK(c, cudaEventRecord(e0, st));
+  for (uint32_t k = 0; k < iterations; ++k) {
+    uint32_t done = 0;
+    cudaError_t e = cache_train_device(c, rec.p, tgt.p, n, st, &done);
+    if (e != cudaSuccess) {
+      c->cfg.steps_per_pass = keep;
+      CCK(c, e);
+    }
+    steps += done;
+  }
+  CCK(c, cudaEventRecord(e1, st));
+  CCK(c, cudaEventSynchronize(e1));
+  c->cfg.steps_per_pass = keep;
+  cudaEventElapsedTime(&ms, e0, e1);
+  if (train_ms) *train_ms = ms / iterations;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CCK(c, cudaGetLastError());
   return PT_OK;
 }
 

@@ -482,6 +482,11 @@ pt_status pt_cache_gradients(pt_cache* cache, const float* records, const float*
  * loss of the last batch goes to *last_loss. */
 pt_status pt_cache_train(pt_cache* cache, const float* records, const float* targets_rgb, uint32_t n,
                          uint32_t steps, float* last_loss);
+/* Device-timed throughput of the cache kernels on n seeded records: mean
+ * milliseconds of one inference over all n, and of one training pass over
+ * them (batches of batch_size), over `iterations` repetitions. Trains the
+ * cache on those records. */
+pt_status pt_cache_benchmark(pt_cache* cache, uint32_t n, uint32_t iterations, double* infer_ms, double* train_ms);
 /* Attaches a new cache to the renderer (NULL detaches it and renders
  * unbiased again). The renderer owns the cache; scenes with participating
  * media are refused (PT_ERR_UNSUPPORTED). */

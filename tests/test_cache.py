@@ -178,3 +178,10 @@ def test_cache_rmse_against_the_fp64_oracle(pt, scenes):
     assert cached[-1][2] < 1.25 * plain[-1][2], (plain[-1], cached[-1])
     # the error keeps falling with more samples (no divergence)
     assert cached[-1][2] < 0.5 * cached[3][2]
+
+
+@pytest.mark.gpu
+def test_cache_benchmark_runs(cache_mod):
+    c = cache_mod.RadianceCache(batch_size=4096)
+    infer_ms, train_ms = c.benchmark(1 << 14, 2)
+    assert infer_ms > 0 and train_ms > 0
