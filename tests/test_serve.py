@@ -40,7 +40,7 @@ def alone(pt, scene, frames):
 def mixed_jobs(jobmix):
     jobs = [(name, getattr(pin_scenes, name)()) for name in
             ("cornell", "disney_ibl", "lights_icosphere", "media", "transparent", "media_transparent",
-             "ortho_sky", "thin_lens_reinhard", "no_tonemap")]
+             "ortho_sky", "thin_lens_reinhard", "no_tonemap", "textured")]
     mix = jobmix.job_mix(n_jobs=6, rate=100.0, seed=5, bases=jobmix.tiny_bases(), min_pixels=8 * 8,
                          max_pixels=48 * 40, max_spp=4)
     jobs += [(f"mix{j.index}_{j.kind}", j.scene) for j in mix]
