@@ -183,25 +183,48 @@ def run_reference(args, scene, workload):
     return 0
 
 
+def progressive_frames(r, abi, frames):
+    """One sample per render call, as an interactive host drives the renderer:
+    device ms per frame with the bounce graph and with the host-driven loop."""
+    out = {}
+    for label, flags in (("graph_ms_per_frame", 0), ("host_loop_ms_per_frame", abi.PROFILE_HOST_LOOP)):
+        r.set_profiling(flags)
+        r.reset()
+        r.render(1)
+        ms = []
+        for _ in range(frames):
+            r.render(1)
+            ms.append(r.stats().render_ms)
+        out[label] = statistics.median(ms)
+    r.set_profiling(0)
+    return out
+
+
 def workloads_leg(pt):
     """The other configurations of the benchmark, each at its full size: the
     Cornell box (also on the host cores, in full), the 2.6M-triangle
     displaced icosphere (with its BVH rebuilt before every frame) and the
     media box."""
     scenes = importlib.import_module("hala-pathtracer_gb300.scenes")
+    abi = importlib.import_module("hala-pathtracer_gb300.abi")
     out = {}
     for name, fn in (("cornell_256_16spp", scenes.cornell), ("displaced_icosphere_1080p_32spp",
                                                                scenes.displaced_icosphere),
                      ("media_box_1024_128spp", scenes.media_box)):
         s = fn()
         r = pt.renderer_for(s)
-        r.render(min(2, s.spp))
+        r.render(s.spp)  # warm-up at the full size: wavefront buffers and the bounce graph
         r.reset()
         r.render(s.spp)
         st = r.stats()
         row = {"paths": st.paths, "render_ms": st.render_ms, "paths_per_s": st.paths / (st.render_ms / 1e3),
                "rays_per_s": (st.closest_rays + st.shadow_rays) / (st.render_ms / 1e3), "triangles": s.num_triangles,
                "bvh_build_ms": st.bvh_build_ms}
+        r.set_profiling(abi.PROFILE_HOST_LOOP)
+        r.reset()
+        r.render(s.spp)
+        row["host_loop_render_ms"] = r.stats().render_ms
+        r.set_profiling(0)
         if name.startswith("displaced"):
             # BVH rebuilt and timed per frame
             r.reset()
@@ -352,6 +375,8 @@ def main():
     ap.add_argument("--no-cache", action="store_true", help="skip the radiance-cache comparison")
     ap.add_argument("--no-workloads", action="store_true", help="skip the other workloads' table")
     ap.add_argument("--serving-jobs", type=int, default=256)
+    ap.add_argument("--bounce-loop", default="graph", choices=["graph", "host"],
+                    help="bounce loop of the timed steps: one CUDA graph per wave, or one host read-back per bounce")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -389,6 +414,8 @@ def main():
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
+    loop_flags = abi.PROFILE_HOST_LOOP if args.bounce_loop == "host" else 0
+    r.set_profiling(loop_flags)
     # warm-up
     for _ in range(args.warmup):
         r.reset()
@@ -400,12 +427,14 @@ def main():
     cs = r.stats()
     nodes_per_ray = cs.trav_nodes / max(cs.closest_rays, 1)
     tris_per_ray = cs.trav_tris / max(cs.closest_rays, 1)
-    r.set_profiling(abi.PROFILE_TRACE_TIMING)
+    r.set_profiling(loop_flags)
+    r.reset()
+    r.render(scene.spp)  # the bounce graph is captured here, outside the timed steps
 
     clocks = ClockSampler(local)
     barrier()
     clocks.start()
-    step_ms, trace_ms, trace_launches, closest, shadow, launches = [], 0.0, 0, 0, 0, 0
+    step_ms, closest, shadow, launches = [], 0, 0, 0
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
@@ -413,8 +442,6 @@ def main():
         r.render(scene.spp)
         st = r.stats()
         step_ms.append(st.render_ms)
-        trace_ms += st.trace_ms
-        trace_launches += st.trace_launches
         closest += st.closest_rays
         shadow += st.shadow_rays
         launches += st.kernel_launches
@@ -424,7 +451,23 @@ def main():
     paths_step = scene.width * scene.height * scene.spp
     value = ws * paths_step * args.steps / (total_ms / 1e3)
     rays_per_s = ws * (closest + shadow) / (total_ms / 1e3)
+
+    # the same steps again with CUDA events around every closest-hit launch
+    # (host-driven bounce loop: events cannot sit inside the bounce graph)
+    r.set_profiling(abi.PROFILE_TRACE_TIMING)
+    host_ms, trace_ms, trace_launches, t_closest = [], 0.0, 0, 0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        r.reset()
+        r.render(scene.spp)
+        st = r.stats()
+        host_ms.append(st.render_ms)
+        trace_ms += st.trace_ms
+        trace_launches += st.trace_launches
+        t_closest += st.closest_rays
     r.set_profiling(0)
+    progressive = progressive_frames(r, abi, 16)
 
     # end to end through the public API, host buffers in and images out
     e2e_ms = []
@@ -451,7 +494,7 @@ def main():
     # roofline of the closest-hit kernel (algorithmic bytes per traced ray)
     bytes_per_ray = 32 + 16 + 128 * nodes_per_ray + 48 * tris_per_ray  # 128-B 4-wide nodes, 48-B triangles
     avg_launch_ms = trace_ms / max(trace_launches, 1)
-    achieved = bytes_per_ray * closest / (trace_ms / 1e3) / 1e9 if trace_ms > 0 else 0.0
+    achieved = bytes_per_ray * t_closest / (trace_ms / 1e3) / 1e9 if trace_ms > 0 else 0.0
     peak, peak_kind = _peaks()
     line = {
         "metric": "paths/s", "value": value, "unit": "paths/s", "n_gpus": ws, "steps": args.steps,
@@ -463,11 +506,15 @@ def main():
                 "ms_per_step": e2e_total / args.steps},
         "roofline": {"kernel": "k_trace (closest hit)", "bound": "hbm", "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": TRACE_DRAM_BYTES_PER_RAY * closest / max(trace_launches, 1),
+                     "traffic": TRACE_DRAM_BYTES_PER_RAY * t_closest / max(trace_launches, 1),
                      "traffic_note": "ncu DRAM bytes per ray (480x270 capture, bounces 0-1) x rays per launch",
                      "bytes_per_ray": bytes_per_ray, "nodes_per_ray": nodes_per_ray, "tris_per_ray": tris_per_ray,
                      "avg_launch_ms": avg_launch_ms, "launches": trace_launches,
-                     "trace_share_of_step": trace_ms / max(total_ms, 1e-9)},
+                     "trace_share_of_step": trace_ms / max(sum(host_ms), 1e-9),
+                     "timing": "events around each launch in K further steps of the same render"},
+        "bounce_loop": {"timed_steps": args.bounce_loop, "ms_per_step": total_ms / args.steps,
+                        "host_loop_ms_per_step": sum(host_ms) / args.steps,
+                        "progressive_1spp": progressive},
         "gpu_launches": launches,
         "clocks": clk,
     }

@@ -162,7 +162,8 @@ class Renderer:
         self._check(self._lib.pt_renderer_set_radiance_cache(self._h, C.byref(cfg) if cfg is not None else None))
 
     def set_profiling(self, flags):
-        """abi.PROFILE_TRACE_TIMING | abi.PROFILE_COUNT, or 0."""
+        """abi.PROFILE_TRACE_TIMING | abi.PROFILE_COUNT | abi.PROFILE_HOST_LOOP, or 0
+        (0: each wave's bounces run as one CUDA graph launch)."""
         self._check(self._lib.pt_renderer_set_profiling(self._h, int(flags)))
 
     def stream(self):

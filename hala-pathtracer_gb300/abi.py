@@ -155,6 +155,7 @@ JOB_STATE_NAMES = {0: "queued", 1: "running", 2: "done", 3: "failed", 4: "cancel
 
 PROFILE_TRACE_TIMING = 1
 PROFILE_COUNT = 2
+PROFILE_HOST_LOOP = 4
 NOALLOC_MAX_TRIANGLES = 65536
 
 

@@ -66,7 +66,7 @@ cudaError_t WaveBuffers::ensure(uint32_t want, bool want_med, bool want_multi) {
   chk(q_diff.ensure(want));
   chk(q_dis.ensure(want));
   chk(q_shadow.ensure(want));
-  chk(counters.ensure(2 * Q_COUNT));
+  chk(counters.ensure(2 * Q_COUNT + G_WORDS));
   chk(rays.ensure(4));
   if (e != cudaSuccess) return e;
   cap = want;
@@ -105,6 +105,14 @@ cudaError_t run_bounces(const DevScene& S, WaveBuffers& W, uint32_t live, uint32
   uint32_t* cnt0 = W.counters.p;
   uint32_t* cnt1 = W.counters.p + Q_COUNT;
   const uint32_t bounce_cap = 4u * max_depth + 4096u;
+  const uint64_t per_bounce = (S.features & PT_FEATURE_MEDIUM) ? 4 : 5;  // trace, logic, 2 shades (, shadow)
+  if (live == 0) {
+    L.bounces = 0;
+    L.timed_out = false;
+    L.launches = 0;
+    return cudaSuccess;
+  }
+  if (L.profiling == 0 && !L.host_loop) return run_bounces_graph(S, W, bounce_cap, L, pinned, st);
   const bool timing = (L.profiling & PT_PROFILE_TRACE_TIMING) != 0 && L.tev;
   uint32_t b = 0;
   for (; b < bounce_cap && live > 0; ++b) {
@@ -137,6 +145,7 @@ cudaError_t run_bounces(const DevScene& S, WaveBuffers& W, uint32_t live, uint32
   }
   L.bounces = b;
   L.timed_out = live > 0;
+  L.launches = per_bounce * b;
   return cudaSuccess;
 }
 
@@ -769,7 +778,6 @@ pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) {
   CK(r, cudaEventRecord(r->ev0, st));
   uint32_t max_bounces = 0;
   uint64_t launches = 0;
-  const uint64_t per_bounce = med ? 4 : 5;  // trace, logic, 2 shades (, shadow)
   BounceLoop L;
   L.profiling = r->profiling;
   L.tev = &r->tev;
@@ -801,7 +809,7 @@ pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) {
     }
     if (L.timed_out) return fail(r, PT_ERR_TIMEOUT, "paths still alive after the bounce cap");
     max_bounces = std::max(max_bounces, L.bounces);
-    launches += 2 + per_bounce * L.bounces;  // camera + accumulate + bounces
+    launches += 2 + L.launches;  // camera + accumulate + bounces
     if (use_cache && P.c_mode == 2) {
       launch_cache_infer(cache_view(r->cache), P.c_rec, P.c_queue, P.c_counts, n, P.rad, P.c_T, st);
       ++launches;
@@ -899,7 +907,8 @@ pt_status pt_renderer_set_radiance_cache(pt_renderer* r, const pt_cache_config* 
 
 pt_status pt_renderer_set_profiling(pt_renderer* r, uint32_t flags) {
   if (!r) return PT_ERR_INVALID_ARG;
-  if (flags & ~(PT_PROFILE_TRACE_TIMING | PT_PROFILE_COUNT)) return fail(r, PT_ERR_INVALID_ARG, "unknown profiling flag");
+  if (flags & ~(PT_PROFILE_TRACE_TIMING | PT_PROFILE_COUNT | PT_PROFILE_HOST_LOOP))
+    return fail(r, PT_ERR_INVALID_ARG, "unknown profiling flag");
   r->profiling = flags;
   return PT_OK;
 }

@@ -62,6 +62,25 @@ struct Buf {
   }
 };
 
+// The bounce loop of one wave as a single CUDA graph launch: a while node
+// whose body is two bounces (even, then odd queue parity). Each bounce is a
+// switch node over grid sizes (4096 x 4^k paths, the last one the wavefront
+// capacity) whose case the previous one-thread control kernel picks from the
+// live-path count, so tail bounces launch small grids without a host round
+// trip. Kernel parameters are captured by value: the graph is rebuilt when
+// the bytes it captured (scene record, path state, queues) change.
+struct BounceGraph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<unsigned char> key;
+  uint32_t builds = 0;  // graphs captured (instantiated or updated) so far
+  BounceGraph() = default;
+  BounceGraph(const BounceGraph&) = delete;
+  BounceGraph& operator=(const BounceGraph&) = delete;
+  ~BounceGraph() { reset(); }
+  void reset();
+};
+
 // Structure-of-arrays state and queues of one wavefront of `cap` paths.
 // `med` adds the medium fields, `multi` the per-path job slot of a shared
 // wavefront.
@@ -76,6 +95,7 @@ struct WaveBuffers {
   Buf<uint32_t> q_a, q_b, q_logic, q_diff, q_dis, q_shadow, counters;
   Buf<unsigned long long> rays;
   PathState P{};
+  BounceGraph graph;
   cudaError_t ensure(uint32_t cap, bool med, bool multi);
   // Bytes one path slot occupies (state + queues), for memory budgets.
   static uint64_t bytes_per_path(bool med, bool multi);
@@ -83,19 +103,29 @@ struct WaveBuffers {
 
 // Options and results of the bounce loop of one wave.
 struct BounceLoop {
-  uint32_t profiling = 0;            // PT_PROFILE_* flags
+  uint32_t profiling = 0;            // PT_PROFILE_* flags (any flag selects the host-driven loop)
+  bool host_loop = false;            // one host round trip per bounce instead of the bounce graph
   std::vector<cudaEvent_t>* tev = nullptr;  // start/stop pairs around closest-hit launches
   size_t ntimed = 0;
   uint32_t bounces = 0;              // bounces run by the last wave
   bool timed_out = false;            // paths still alive after the bounce cap
+  uint64_t launches = 0;             // kernels launched by the last wave's bounces
 };
 
 // Runs bounce after bounce of the `live` paths queued in W.q_a (the camera
 // kernel wrote their count to counters[Q_COUNT + Q_NEXT]) until no path
-// continues. The host reads the continuing-path count once per bounce
-// through `pinned` (one uint32_t of pinned host memory).
+// continues, at most 4 * max_depth + 4096 bounces. Without profiling flags
+// the loop is one launch of W.graph and one read-back of (bounces, live);
+// otherwise the host reads the continuing-path count after every bounce.
+// `pinned` is at least two uint32_t of pinned host memory.
 cudaError_t run_bounces(const DevScene& S, WaveBuffers& W, uint32_t live, uint32_t max_depth, BounceLoop& L,
                         uint32_t* pinned, cudaStream_t st);
+
+// The graph form of run_bounces (pt_graph.cu). Control words live after the
+// two counter sets: counters[2 * Q_COUNT + G_*].
+enum GraphWord : uint32_t { G_DONE = 0, G_LIVE = 1, G_GO = 2, G_WORDS = 4 };
+cudaError_t run_bounces_graph(const DevScene& S, WaveBuffers& W, uint32_t bounce_cap, BounceLoop& L,
+                              uint32_t* pinned, cudaStream_t st);
 
 }  // namespace hpt
 

@@ -333,7 +333,7 @@ bool plan_wave(pt_server* s, std::vector<Segment>& segs, uint32_t cap) {
 }
 
 // Runs one wavefront on the server stream (render thread, no lock held).
-cudaError_t run_wave(pt_server* s, std::vector<Segment>& segs, uint32_t total, uint32_t* bounces, bool* timed_out,
+cudaError_t run_wave(pt_server* s, std::vector<Segment>& segs, uint32_t total, uint64_t* launches, bool* timed_out,
                      uint64_t rays[2], float* ms) {
   cudaError_t e;
   cudaStream_t st = s->stream;
@@ -370,9 +370,15 @@ cudaError_t run_wave(pt_server* s, std::vector<Segment>& segs, uint32_t total, u
                       s->W.counters.p + Q_COUNT + Q_NEXT, st);
   uint32_t max_depth = 0;
   for (Segment& g : segs) max_depth = std::max(max_depth, g.job->r->cfg.max_depth);
+  // The shared-wavefront kernels read each path's scene from the slot table;
+  // the scene record they take by value only carries the feature set, so
+  // the bounce graph captured for one feature set serves every wavefront of it.
+  DevScene S;
+  std::memset(&S, 0, sizeof(S));
+  S.features = segs[0].job->r->view.features;
   BounceLoop L;
-  if ((e = run_bounces(segs[0].job->r->view, s->W, total, max_depth, L, s->pinned, st)) != cudaSuccess) return e;
-  *bounces = L.bounces;
+  if ((e = run_bounces(S, s->W, total, max_depth, L, s->pinned, st)) != cudaSuccess) return e;
+  *launches = L.launches;
   *timed_out = L.timed_out;
   if (L.timed_out) return cudaSuccess;
   for (Segment& g : segs) {
@@ -428,11 +434,11 @@ void render_loop(pt_server* s) {
     uint32_t total = 0;
     for (const Segment& g : segs) total += g.count;
     lk.unlock();
-    uint32_t bounces = 0;
+    uint64_t bounce_launches = 0;
     bool timed_out = false;
     uint64_t rays[2] = {0, 0};
     float ms = 0.0f;
-    cudaError_t e = run_wave(s, segs, total, &bounces, &timed_out, rays, &ms);
+    cudaError_t e = run_wave(s, segs, total, &bounce_launches, &timed_out, rays, &ms);
     lk.lock();
     ++s->st.wavefronts;
     if (e != cudaSuccess || timed_out) {
@@ -448,12 +454,11 @@ void render_loop(pt_server* s) {
       }
       continue;
     }
-    const bool med = (segs[0].job->features & PT_FEATURE_MEDIUM) != 0;
     s->st.paths += total;
     s->st.closest_rays += rays[0];
     s->st.shadow_rays += rays[1];
     s->st.busy_ms += ms;
-    s->st.kernel_launches += 1 + (med ? 4 : 5) * (uint64_t)bounces;
+    s->st.kernel_launches += 1 + bounce_launches;  // camera + bounces
     for (Segment& g : segs) {
       JobPtr j = g.job;
       j->done += g.count;

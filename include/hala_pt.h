@@ -215,6 +215,10 @@ typedef struct pt_stats {
 /* Profiling switches for pt_renderer_set_profiling. */
 #define PT_PROFILE_TRACE_TIMING 1u  /* CUDA events around every closest-hit launch */
 #define PT_PROFILE_COUNT 2u         /* count traversal work (slower counting kernels) */
+/* Any flag above, or this one, drives the bounce loop from the host (one
+ * read-back of the live-path count per bounce) instead of launching each
+ * wave's bounces as one CUDA graph; the images are the same either way. */
+#define PT_PROFILE_HOST_LOOP 4u
 
 #define PT_FEATURE_MEDIUM 1u
 #define PT_FEATURE_VOL_MIS 2u

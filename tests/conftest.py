@@ -22,6 +22,11 @@ def pt():
 
 
 @pytest.fixture(scope="session")
+def abi(pt):
+    return importlib.import_module("hala-pathtracer_gb300.abi")
+
+
+@pytest.fixture(scope="session")
 def scenes(pt):
     return importlib.import_module("hala-pathtracer_gb300.scenes")
 
