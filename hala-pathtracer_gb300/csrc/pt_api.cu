@@ -505,7 +505,10 @@ pt_status hpt::renderer_create_with_priority(const pt_tracer_config* cfg, int pr
   pt_renderer* r = new pt_renderer();
   r->cfg = *cfg;
   if (cudaStreamCreateWithPriority(&r->stream, cudaStreamNonBlocking, priority) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&r->side, cudaStreamNonBlocking, priority) != cudaSuccess ||
       cudaEventCreate(&r->ev0) != cudaSuccess || cudaEventCreate(&r->ev1) != cudaSuccess ||
+      cudaEventCreateWithFlags(&r->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&r->ev_join, cudaEventDisableTiming) != cudaSuccess ||
       cudaMallocHost(&r->pinned, 64) != cudaSuccess) {
     pt_renderer_destroy(r);
     return PT_ERR_CUDA;
@@ -529,8 +532,11 @@ extern "C" {
 void pt_renderer_destroy(pt_renderer* r) {
   if (!r) return;
   if (r->stream) cudaStreamSynchronize(r->stream);
+  if (r->side) cudaStreamSynchronize(r->side);
   if (r->ev0) cudaEventDestroy(r->ev0);
   if (r->ev1) cudaEventDestroy(r->ev1);
+  if (r->ev_fork) cudaEventDestroy(r->ev_fork);
+  if (r->ev_join) cudaEventDestroy(r->ev_join);
   if (r->pinned) cudaFreeHost(r->pinned);
   for (cudaEvent_t e : r->tev) cudaEventDestroy(e);
   if (r->cache) pt_cache_destroy(r->cache);
@@ -636,10 +642,14 @@ pt_status pt_renderer_set_envmap(pt_renderer* r, const float* rgb, uint32_t w, u
     r->env_map = false;
     return PT_OK;
   }
-  std::vector<float4> px((size_t)w * h);
-  for (size_t i = 0; i < px.size(); ++i) px[i] = make_float4(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2], 0.0f);
-  CK(r, r->env.ensure(px.size()));
-  CK(r, cudaMemcpyAsync(r->env.p, px.data(), px.size() * sizeof(float4), cudaMemcpyHostToDevice, r->stream));
+  // RGB as given, widened to RGBA on the device
+  const size_t n = (size_t)w * h;
+  Buf<float> rgb_dev;
+  CK(r, rgb_dev.ensure(3 * n));
+  CK(r, r->env.ensure(n));
+  CK(r, cudaMemcpyAsync(rgb_dev.p, rgb, 3 * n * sizeof(float), cudaMemcpyHostToDevice, r->stream));
+  launch_env_widen(rgb_dev.p, r->env.p, n, r->stream);
+  CK(r, cudaGetLastError());
   CK(r, cudaStreamSynchronize(r->stream));
   r->env_map = true;
   r->env_w = w;
@@ -696,6 +706,37 @@ pt_status pt_renderer_commit(pt_renderer* r) {
   }
   r->features = f;
   cudaStream_t st = r->stream;
+  // environment alias tables (FP64, one thread per row) on the side stream,
+  // concurrently with the BVH build; joined before the commit returns
+  Buf<double> q, sums, tot;
+  Buf<uint32_t> stacks;
+  // Declared after the scratch buffers so that on every return the main
+  // stream waits for the side stream before their stream-ordered frees.
+  struct Join {
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev = nullptr;
+    ~Join() {
+      if (st) cudaStreamWaitEvent(st, ev, 0);
+    }
+  } join;
+  if (r->env_map) {
+    const size_t WH = (size_t)r->env_w * r->env_h;
+    CK(r, q.ensure(2 * WH));
+    CK(r, sums.ensure(r->env_h));
+    CK(r, tot.ensure(1));
+    CK(r, stacks.ensure(2 * WH));
+    CK(r, r->alias_rows.ensure(r->env_h));
+    CK(r, r->alias_cols.ensure(WH));
+    CK(r, cudaEventRecord(r->ev_fork, st));
+    CK(r, cudaStreamWaitEvent(r->side, r->ev_fork, 0));
+    launch_env_tables(r->env.p, r->env_w, r->env_h, r->alias_rows.p, r->alias_cols.p, q.p, stacks.p, sums.p, tot.p,
+                      r->side);
+    const cudaError_t le = cudaGetLastError();
+    CK(r, cudaEventRecord(r->ev_join, r->side));
+    join.st = st;
+    join.ev = r->ev_join;
+    CK(r, le);
+  }
   CK(r, r->tri_sorted.ensure(3 * (size_t)std::max<uint32_t>(r->ntris, 1)));
   CK(r, cudaEventRecord(r->ev0, st));
   if (r->ntris > 0) {
@@ -725,18 +766,7 @@ pt_status pt_renderer_commit(pt_renderer* r) {
   r->stats.bvh_nodes = r->nnodes;
   r->stats.triangles = r->ntris;
   if (r->env_map) {
-    const size_t WH = (size_t)r->env_w * r->env_h;
-    Buf<double> q, sums, tot;
-    Buf<uint32_t> stacks;
-    CK(r, q.ensure(2 * WH));
-    CK(r, sums.ensure(r->env_h));
-    CK(r, tot.ensure(1));
-    CK(r, stacks.ensure(2 * WH));
-    CK(r, r->alias_rows.ensure(r->env_h));
-    CK(r, r->alias_cols.ensure(WH));
-    launch_env_tables(r->env.p, r->env_w, r->env_h, r->alias_rows.p, r->alias_cols.p, q.p, stacks.p, sums.p, tot.p,
-                      st);
-    CK(r, cudaGetLastError());
+    CK(r, cudaStreamWaitEvent(st, r->ev_join, 0));
     CK(r, cudaMemcpyAsync(&r->env_total, tot.p, sizeof(double), cudaMemcpyDeviceToHost, st));
     CK(r, cudaStreamSynchronize(st));
   }

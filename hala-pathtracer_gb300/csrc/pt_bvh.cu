@@ -78,36 +78,89 @@ __device__ __forceinline__ float warp_max(float v) {
   return v;
 }
 
+// Bins one triangle per valid lane on the three axes into shared bins
+// (count, min box, max box as ordered ints). Lanes of the warp that fall into
+// the same bin are merged first (__match_any_sync, then reductions over that
+// group) and the lowest of them does the atomics: in the multi-block top
+// levels neighbouring triangles are close in space and would otherwise hit
+// one bin with 32 atomics in a row (2.4x faster there; in the small tasks of
+// k_level and k_subtree, where few lanes share a bin, the plain atomics are
+// faster). All 32 lanes call it; cext[] is uniform over the warp. Integer
+// counts and min/max: the bins do not depend on the order.
+__device__ __forceinline__ void bin_warp(bool valid, float4 c, float4 lo, float4 hi, const float clo[3],
+                                         const float cext[3], int (*bcnt)[NB], int (*bmin)[NB][3],
+                                         int (*bmax)[NB][3]) {
+  const unsigned act = __ballot_sync(0xffffffffu, valid);
+  if (!valid) return;
+  const int lane = threadIdx.x & 31;
+  const float cc[3] = {c.x, c.y, c.z};
+  const int ilo[3] = {f2o(lo.x), f2o(lo.y), f2o(lo.z)};
+  const int ihi[3] = {f2o(hi.x), f2o(hi.y), f2o(hi.z)};
+  for (int a = 0; a < 3; ++a) {
+    if (!(cext[a] > 0.0f)) continue;
+    const int b = min(NB - 1, max(0, (int)((cc[a] - clo[a]) * ((float)NB / cext[a]))));
+    const unsigned grp = __match_any_sync(act, b);
+    int gl[3], gh[3];
+    for (int k = 0; k < 3; ++k) {
+      gl[k] = __reduce_min_sync(grp, ilo[k]);
+      gh[k] = __reduce_max_sync(grp, ihi[k]);
+    }
+    if (lane == __ffs(grp) - 1) {
+      atomicAdd(&bcnt[a][b], __popc(grp));
+      for (int k = 0; k < 3; ++k) {
+        atomicMin(&bmin[a][b][k], gl[k]);
+        atomicMax(&bmax[a][b][k], gh[k]);
+      }
+    }
+  }
+}
+
 constexpr uint32_t MAX_LARGE_TASKS = 1024;  // capacity of the per-level large-task list
 
-// Appends the two children of a split task to the next level's task list,
-// or to the list of large tasks (count > large_min) that the multi-block
-// path handles.
-__device__ __forceinline__ void push_children(uint32_t c, const BuildTask& t, uint32_t nleft, BuildTask* next_tasks,
-                                              uint32_t* next_count, BuildTask* next_large,
-                                              uint32_t* next_large_count, uint32_t large_min) {
+// Where the children of a split task go: the next level's list (one block
+// per task), the multi-block list (more than large_min triangles), or the
+// whole-subtree list (at most sub_max triangles, built to the leaves by one
+// warp each after the levels; `dst_parity` records which id buffer holds
+// their ranges). A full list spills into the next level's list, which builds
+// the same tree more slowly.
+struct ChildLists {
+  BuildTask* tasks;
+  uint32_t* count;
+  BuildTask* large = nullptr;
+  uint32_t* large_count = nullptr;
+  uint32_t large_min = 0xFFFFFFFFu;
+  BuildTask* sub = nullptr;
+  uint32_t* sub_count = nullptr;
+  uint32_t sub_max = 0;
+  uint32_t sub_cap = 0;
+  uint32_t dst_parity = 0;
+};
+
+__device__ __forceinline__ void push_children(uint32_t c, const BuildTask& t, uint32_t nleft, const ChildLists& L) {
   const BuildTask kids[2] = {BuildTask{c, t.start, nleft, 0}, BuildTask{c + 1, t.start + nleft, t.count - nleft, 0}};
   for (int k = 0; k < 2; ++k) {
-    if (kids[k].count > large_min) {
-      const uint32_t q = atomicAdd(next_large_count, 1u);
-      if (q < MAX_LARGE_TASKS) {
-        next_large[q] = kids[k];
+    if (L.sub && kids[k].count <= L.sub_max) {
+      const uint32_t q = atomicAdd(L.sub_count, 1u);
+      if (q < L.sub_cap) {
+        L.sub[q] = BuildTask{kids[k].node, kids[k].start, kids[k].count, L.dst_parity};
         continue;
       }
-      // the large list is full: the one-block path handles it (slower, same tree)
     }
-    next_tasks[atomicAdd(next_count, 1u)] = kids[k];
+    if (L.large && kids[k].count > L.large_min) {
+      const uint32_t q = atomicAdd(L.large_count, 1u);
+      if (q < MAX_LARGE_TASKS) {
+        L.large[q] = kids[k];
+        continue;
+      }
+    }
+    L.tasks[atomicAdd(L.count, 1u)] = kids[k];
   }
 }
 
 __global__ void __launch_bounds__(BUILD_THREADS) k_level(const BuildTask* tasks, const uint32_t* ntasks_ptr,
                                                          const uint32_t* src, uint32_t* dst, uint32_t* final_ids,
                                                          const float4* tlo, const float4* thi, const float4* tc,
-                                                         BuildNode* nodes, uint32_t* node_counter,
-                                                         BuildTask* next_tasks, uint32_t* next_count,
-                                                         BuildTask* next_large = nullptr,
-                                                         uint32_t* next_large_count = nullptr,
-                                                         uint32_t large_min = 0xFFFFFFFFu) {
+                                                         BuildNode* nodes, uint32_t* node_counter, ChildLists next) {
   __shared__ float red[12][BUILD_THREADS / 32];
   __shared__ float box[12];
   __shared__ int bcnt[3][NB];
@@ -282,8 +335,285 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_level(const BuildTask* tasks,
     nd.right = (int32_t)(c + 1);
     nd.start = 0;
     nd.count = 0;
-    push_children(c, t, nleft, next_tasks, next_count, next_large, next_large_count, large_min);
+    push_children(c, t, nleft, next);
   }
+}
+
+// ---------------------------------------------------------------------------
+// Whole subtrees. The deep levels of a big scene hold hundreds of thousands
+// of tasks of a few triangles, and one block per task per level leaves most
+// of each block idle. A task of at most SUBTREE_MAX triangles is therefore
+// built down to its leaves by one warp, with the same bounds, bins, SAH
+// costs, leaf rule and stable partition as k_level, so the tree is the same.
+// The warp first copies its triangles' boxes and centroids into shared
+// memory; inside the subtree it permutes 16-bit local indices, and only the
+// leaves go back to the global ids. It continues with the smaller child and
+// keeps the larger one on a short stack: every stacked task is at least as
+// large as the current one, so the stack holds at most log2(SUBTREE_MAX)
+// entries, and a subtree of c triangles has fewer than 2c nodes, which
+// bounds the loop.
+constexpr uint32_t SUBTREE_MAX = 256;
+constexpr int SUB_WARPS = 8;
+constexpr int SUB_STACK = 16;
+
+// Shared memory of one warp of k_subtree.
+struct SubtreeSmem {
+  float lx[SUBTREE_MAX], ly[SUBTREE_MAX], lz[SUBTREE_MAX];
+  float hx[SUBTREE_MAX], hy[SUBTREE_MAX], hz[SUBTREE_MAX];
+  float cx[SUBTREE_MAX], cy[SUBTREE_MAX], cz[SUBTREE_MAX];
+  uint32_t gid[SUBTREE_MAX];
+  uint16_t lid[2][SUBTREE_MAX];
+  int bcnt[3][NB];
+  int bmin[3][NB][3];
+  int bmax[3][NB][3];
+  BuildTask stack[SUB_STACK];
+};
+constexpr size_t SUBTREE_SMEM = SUB_WARPS * sizeof(SubtreeSmem);
+
+// The SAH costs of all 3 x 15 planes of one task from its bins by segmented
+// scans: lanes 0-15 hold the bins of one axis and lanes 16-31 of the next
+// (axes 0 and 1, then axis 2). Each lane's inclusive prefix is the left side
+// of its plane and its right neighbour's inclusive suffix the right side.
+// min/max are exact and an empty bin holds the identity box, so the sides,
+// counts and costs equal k_level's per-plane loops bit for bit. Returns the
+// lane's cheapest plane (strictly lower cost wins, so ties keep the lower
+// plane index).
+__device__ __forceinline__ void sah_scan(const SubtreeSmem& S, const float cext[3], int lane, float& bc, int& bi) {
+  const unsigned FULL = 0xffffffffu;
+  bc = 3.0e38f;
+  bi = -1;
+  const int half = lane >> 4, b = lane & 15;
+  for (int pass = 0; pass < 2; ++pass) {
+    const int a = 2 * pass + half;
+    const bool act = a < 3;
+    int cnt = 0;
+    float mn[3] = {1e30f, 1e30f, 1e30f}, mx[3] = {-1e30f, -1e30f, -1e30f};
+    if (act) {
+      cnt = S.bcnt[a][b];
+      for (int q = 0; q < 3; ++q) {
+        mn[q] = o2f(S.bmin[a][b][q]);
+        mx[q] = o2f(S.bmax[a][b][q]);
+      }
+    }
+    int pc = cnt, sc = cnt;
+    float pmn[3] = {mn[0], mn[1], mn[2]}, pmx[3] = {mx[0], mx[1], mx[2]};
+    float smn[3] = {mn[0], mn[1], mn[2]}, smx[3] = {mx[0], mx[1], mx[2]};
+    for (int o = 1; o < 16; o <<= 1) {
+      const int c_up = __shfl_up_sync(FULL, pc, o, 16), c_dn = __shfl_down_sync(FULL, sc, o, 16);
+      float u_mn[3], u_mx[3], d_mn[3], d_mx[3];
+      for (int q = 0; q < 3; ++q) {
+        u_mn[q] = __shfl_up_sync(FULL, pmn[q], o, 16);
+        u_mx[q] = __shfl_up_sync(FULL, pmx[q], o, 16);
+        d_mn[q] = __shfl_down_sync(FULL, smn[q], o, 16);
+        d_mx[q] = __shfl_down_sync(FULL, smx[q], o, 16);
+      }
+      if (b >= o) {
+        pc += c_up;
+        for (int q = 0; q < 3; ++q) { pmn[q] = fminf(pmn[q], u_mn[q]); pmx[q] = fmaxf(pmx[q], u_mx[q]); }
+      }
+      if (b + o < 16) {
+        sc += c_dn;
+        for (int q = 0; q < 3; ++q) { smn[q] = fminf(smn[q], d_mn[q]); smx[q] = fmaxf(smx[q], d_mx[q]); }
+      }
+    }
+    const int rc = __shfl_down_sync(FULL, sc, 1, 16);
+    float rmn[3], rmx[3];
+    for (int q = 0; q < 3; ++q) {
+      rmn[q] = __shfl_down_sync(FULL, smn[q], 1, 16);
+      rmx[q] = __shfl_down_sync(FULL, smx[q], 1, 16);
+    }
+    if (act && b < NB - 1 && cext[a] > 0.0f && pc > 0 && rc > 0) {
+      const float cost = box_area(pmn[0], pmn[1], pmn[2], pmx[0], pmx[1], pmx[2]) * pc +
+                         box_area(rmn[0], rmn[1], rmn[2], rmx[0], rmx[1], rmx[2]) * rc;
+      if (cost < bc) {
+        bc = cost;
+        bi = a * (NB - 1) + b;
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(SUB_WARPS * 32) k_subtree(const BuildTask* tasks, const uint32_t* ntasks_ptr,
+                                                            uint32_t cap, const uint32_t* ids_a,
+                                                            const uint32_t* ids_b, uint32_t* final_ids,
+                                                            const float4* tlo, const float4* thi, const float4* tc,
+                                                            BuildNode* nodes, uint32_t* node_counter,
+                                                            uint32_t* error_flag) {
+  extern __shared__ __align__(16) unsigned char sub_smem[];
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const uint32_t ti = blockIdx.x * SUB_WARPS + w;
+  if (ti >= min(*ntasks_ptr, cap)) return;  // warp-uniform
+  SubtreeSmem& S = reinterpret_cast<SubtreeSmem*>(sub_smem)[w];
+  const BuildTask root = tasks[ti];
+  if (root.count > SUBTREE_MAX) {  // never pushed (see ChildLists); reported, not built
+    if (lane == 0) atomicExch(error_flag, 3u);
+    return;
+  }
+  {
+    const uint32_t* src = root.pad ? ids_b : ids_a;
+    for (uint32_t k = lane; k < root.count; k += 32) {
+      const uint32_t id = src[root.start + k];
+      const float4 lo = tlo[id], hi = thi[id], c = tc[id];
+      S.lx[k] = lo.x; S.ly[k] = lo.y; S.lz[k] = lo.z;
+      S.hx[k] = hi.x; S.hy[k] = hi.y; S.hz[k] = hi.z;
+      S.cx[k] = c.x;  S.cy[k] = c.y;  S.cz[k] = c.z;
+      S.gid[k] = id;
+      S.lid[0][k] = (uint16_t)k;
+    }
+  }
+  __syncwarp();
+  // The subtree's nodes come from one reservation: its splits number at most
+  // count - 1, two nodes each. Unused slots are marked as leaves at the end
+  // so that the layout pass reads only valid links.
+  const uint32_t reserved = 2u * (root.count - 1u);
+  uint32_t nbase = 0, used = 0;
+  if (lane == 0 && reserved > 0) nbase = atomicAdd(node_counter, reserved);
+  nbase = __shfl_sync(FULL, nbase, 0);
+  // tasks below use start relative to the subtree and pad = local buffer
+  BuildTask t{root.node, 0u, root.count, 0u};
+  int sp = 0;
+  for (uint32_t iter = 0; iter < 2 * SUBTREE_MAX; ++iter) {
+    const uint16_t* src = S.lid[t.pad];
+    uint16_t* dst = S.lid[t.pad ^ 1u];
+    const uint32_t end = t.start + t.count;
+    // 1. box and centroid box (every value below is uniform over the warp)
+    float v[12];
+    for (int k = 0; k < 6; ++k) { v[k] = 1e30f; v[6 + k] = -1e30f; }
+    for (uint32_t i = t.start + lane; i < end; i += 32) {
+      const uint32_t j = src[i];
+      v[0] = fminf(v[0], S.lx[j]); v[1] = fminf(v[1], S.ly[j]); v[2] = fminf(v[2], S.lz[j]);
+      v[3] = fminf(v[3], S.cx[j]); v[4] = fminf(v[4], S.cy[j]); v[5] = fminf(v[5], S.cz[j]);
+      v[6] = fmaxf(v[6], S.hx[j]); v[7] = fmaxf(v[7], S.hy[j]); v[8] = fmaxf(v[8], S.hz[j]);
+      v[9] = fmaxf(v[9], S.cx[j]); v[10] = fmaxf(v[10], S.cy[j]); v[11] = fmaxf(v[11], S.cz[j]);
+    }
+    for (int k = 0; k < 6; ++k) { v[k] = warp_min(v[k]); v[6 + k] = warp_max(v[6 + k]); }
+    BuildNode& nd = nodes[t.node];
+    if (lane == 0) {
+      nd.lo[0] = v[0]; nd.lo[1] = v[1]; nd.lo[2] = v[2];
+      nd.hi[0] = v[6]; nd.hi[1] = v[7]; nd.hi[2] = v[8];
+    }
+    const float clo[3] = {v[3], v[4], v[5]};
+    const float cext[3] = {v[9] - v[3], v[10] - v[4], v[11] - v[5]};
+    bool leaf = t.count <= 2;
+    int best = -1;
+    if (!leaf) {
+      // 2. bins
+      for (int k = lane; k < 3 * NB; k += 32) {
+        int a = k / NB, b = k % NB;
+        S.bcnt[a][b] = 0;
+        for (int c = 0; c < 3; ++c) { S.bmin[a][b][c] = f2o(1e30f); S.bmax[a][b][c] = f2o(-1e30f); }
+      }
+      __syncwarp();
+      for (uint32_t i = t.start + lane; i < end; i += 32) {
+        const uint32_t j = src[i];
+        const float cc[3] = {S.cx[j], S.cy[j], S.cz[j]};
+        const int ilo[3] = {f2o(S.lx[j]), f2o(S.ly[j]), f2o(S.lz[j])};
+        const int ihi[3] = {f2o(S.hx[j]), f2o(S.hy[j]), f2o(S.hz[j])};
+        for (int a = 0; a < 3; ++a) {
+          if (!(cext[a] > 0.0f)) continue;
+          int b = min(NB - 1, max(0, (int)((cc[a] - clo[a]) * ((float)NB / cext[a]))));
+          atomicAdd(&S.bcnt[a][b], 1);
+          for (int k = 0; k < 3; ++k) {
+            atomicMin(&S.bmin[a][b][k], ilo[k]);
+            atomicMax(&S.bmax[a][b][k], ihi[k]);
+          }
+        }
+      }
+      __syncwarp();
+      // 3. SAH cost of every plane (lane k: planes k and k + 32), then the
+      // cheapest, ties to the lower plane index as k_level scans them
+      float bc;
+      int bi;
+      sah_scan(S, cext, lane, bc, bi);
+      for (int o = 16; o > 0; o >>= 1) {
+        const float oc = __shfl_xor_sync(FULL, bc, o);
+        const int oi = __shfl_xor_sync(FULL, bi, o);
+        if (oi >= 0 && (oc < bc || (oc == bc && (bi < 0 || oi < bi)))) { bc = oc; bi = oi; }
+      }
+      const float area = box_area(v[0], v[1], v[2], v[6], v[7], v[8]);
+      if (bi < 0) best = (t.count <= (uint32_t)LEAF_MAX) ? -2 : -1;  // -2 leaf, -1 median split
+      else if (t.count <= (uint32_t)SAH_LEAF_MAX && area * t.count <= bc + 0.5f * area) best = -2;
+      else best = bi;
+      leaf = best == -2;
+    }
+    if (!leaf) {
+      // 4. stable partition into the other local buffer
+      uint32_t nleft;
+      if (best < 0) {
+        nleft = t.count / 2;
+        for (uint32_t i = t.start + lane; i < end; i += 32) dst[i] = src[i];
+      } else {
+        const int a = best / (NB - 1), s = best % (NB - 1);
+        nleft = 0;
+        for (int b = 0; b <= s; ++b) nleft += (uint32_t)S.bcnt[a][b];
+        const float scale = (float)NB / cext[a];
+        const float* ca = a == 0 ? S.cx : (a == 1 ? S.cy : S.cz);
+        const unsigned lt = (1u << lane) - 1u;
+        uint32_t lbase = 0, rbase = 0;
+        for (uint32_t base = t.start; base < end; base += 32) {
+          const uint32_t i = base + lane;
+          const bool valid = i < end;
+          const uint16_t j = valid ? src[i] : (uint16_t)0;
+          bool left = false;
+          if (valid) {
+            int b = min(NB - 1, max(0, (int)((ca[j] - clo[a]) * scale)));
+            left = b <= s;
+          }
+          const unsigned m = __ballot_sync(FULL, left), mv = __ballot_sync(FULL, valid);
+          if (valid) {
+            if (left) dst[t.start + lbase + __popc(m & lt)] = j;
+            else dst[t.start + nleft + rbase + __popc(mv & ~m & lt)] = j;
+          }
+          lbase += __popc(m);
+          rbase += __popc(mv & ~m);
+        }
+      }
+      if (used + 2 > reserved) {  // cannot happen (see above); reported, never written out of bounds
+        if (lane == 0) atomicExch(error_flag, 4u);
+        return;
+      }
+      const uint32_t c = nbase + used;
+      used += 2;
+      if (lane == 0) {
+        nd.left = (int32_t)c;
+        nd.right = (int32_t)(c + 1);
+        nd.start = 0;
+        nd.count = 0;
+      }
+      const BuildTask L{c, t.start, nleft, t.pad ^ 1u};
+      const BuildTask R{c + 1, t.start + nleft, t.count - nleft, t.pad ^ 1u};
+      const bool go_left = L.count <= R.count;
+      if (sp >= SUB_STACK) {  // cannot happen (see above); reported, never written out of bounds
+        if (lane == 0) atomicExch(error_flag, 1u);
+        return;
+      }
+      __syncwarp();
+      if (lane == 0) S.stack[sp] = go_left ? R : L;
+      __syncwarp();
+      ++sp;
+      t = go_left ? L : R;
+      continue;
+    }
+    for (uint32_t i = t.start + lane; i < end; i += 32) final_ids[root.start + i] = S.gid[src[i]];
+    if (lane == 0) {
+      nd.left = -1;
+      nd.right = -1;
+      nd.start = root.start + t.start;
+      nd.count = t.count;
+    }
+    if (sp == 0) {
+      for (uint32_t k = used + lane; k < reserved; k += 32) {
+        nodes[nbase + k].left = -1;
+        nodes[nbase + k].count = 0;
+      }
+      return;
+    }
+    --sp;
+    t = S.stack[sp];
+    __syncwarp();
+  }
+  if (lane == 0) atomicExch(error_flag, 2u);  // loop bound reached: cannot happen for a well-formed task
 }
 
 // ---------------------------------------------------------------------------
@@ -294,7 +624,7 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_level(const BuildTask* tasks,
 // integer atomics, one thread per task picks the plane, and the stable
 // partition uses per-chunk left counts (each chunk sums the counts of the
 // chunks before it).
-constexpr uint32_t LARGE_TASK = 1u << 15;
+constexpr uint32_t LARGE_TASK = 1u << 13;
 constexpr uint32_t CHUNK = 4096;
 constexpr uint32_t MAX_LARGE = MAX_LARGE_TASKS;
 
@@ -386,21 +716,17 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_large_bin(const BuildTask* la
     for (int c = 0; c < 3; ++c) { bmin[a][b][c] = f2o(1e30f); bmax[a][b][c] = f2o(-1e30f); }
   }
   __syncthreads();
-  for (uint32_t i = b0 + tid; i < b1; i += BUILD_THREADS) {
-    uint32_t id = src[i];
-    float4 c = tc[id], lo = tlo[id], hi = thi[id];
-    const float cc[3] = {c.x, c.y, c.z};
-    const int ilo[3] = {f2o(lo.x), f2o(lo.y), f2o(lo.z)};
-    const int ihi[3] = {f2o(hi.x), f2o(hi.y), f2o(hi.z)};
-    for (int a = 0; a < 3; ++a) {
-      if (!(cext[a] > 0.0f)) continue;
-      int b = min(NB - 1, max(0, (int)((cc[a] - clo[a]) * ((float)NB / cext[a]))));
-      atomicAdd(&bcnt[a][b], 1);
-      for (int k = 0; k < 3; ++k) {
-        atomicMin(&bmin[a][b][k], ilo[k]);
-        atomicMax(&bmax[a][b][k], ihi[k]);
-      }
+  for (uint32_t base = b0; base < b1; base += BUILD_THREADS) {
+    const uint32_t i = base + tid;
+    const bool valid = i < b1;
+    float4 c = make_float4(0.f, 0.f, 0.f, 0.f), lo = c, hi = c;
+    if (valid) {
+      const uint32_t id = src[i];
+      c = tc[id];
+      lo = tlo[id];
+      hi = thi[id];
     }
+    bin_warp(valid, c, lo, hi, clo, cext, bcnt, bmin, bmax);
   }
   __syncthreads();
   for (int k = tid; k < 3 * NB; k += BUILD_THREADS) {
@@ -414,43 +740,51 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_large_bin(const BuildTask* la
   }
 }
 
-// One thread per large task: SAH over the merged bins (the same cost as
-// k_level), node box, children.
+// One warp per large task: SAH over the merged bins (the same costs as
+// k_level; lane k prices planes k and k + 32, the cheapest wins with ties to
+// the lower plane index), node box, children.
 __global__ void k_large_split(const BuildTask* large, uint32_t nlarge, LargeState* st, BuildNode* nodes,
-                              uint32_t* node_counter, BuildTask* next_tasks, uint32_t* next_count,
-                              BuildTask* next_large, uint32_t* next_large_count, uint32_t large_min) {
-  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= nlarge) return;
+                              uint32_t* node_counter, ChildLists next) {
+  const unsigned FULL = 0xffffffffu;
+  const uint32_t j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (j >= nlarge) return;  // warp-uniform
   const BuildTask t = large[j];
   LargeState& S = st[j];
   float box[12];
   for (int k = 0; k < 12; ++k) box[k] = o2f(S.box[k]);
   BuildNode& nd = nodes[t.node];
-  nd.lo[0] = box[0]; nd.lo[1] = box[1]; nd.lo[2] = box[2];
-  nd.hi[0] = box[6]; nd.hi[1] = box[7]; nd.hi[2] = box[8];
-  int bi = -1;
   float bc = 3.0e38f;
-  for (int a = 0; a < 3; ++a) {
+  int bi = -1;
+  for (int k = lane; k < 3 * (NB - 1); k += 32) {
+    const int a = k / (NB - 1), s = k % (NB - 1);
     if (!(box[9 + a] - box[3 + a] > 0.0f)) continue;
-    for (int s = 0; s < NB - 1; ++s) {
-      float l[6] = {1e30f, 1e30f, 1e30f, -1e30f, -1e30f, -1e30f}, r[6] = {1e30f, 1e30f, 1e30f, -1e30f, -1e30f, -1e30f};
-      int nl = 0, nr = 0;
-      for (int b = 0; b < NB; ++b) {
-        float* dstb = b <= s ? l : r;
-        int cnt = S.bcnt[a][b];
-        if (cnt == 0) continue;
-        if (b <= s) nl += cnt; else nr += cnt;
-        for (int k = 0; k < 3; ++k) {
-          dstb[k] = fminf(dstb[k], o2f(S.bmin[a][b][k]));
-          dstb[3 + k] = fmaxf(dstb[3 + k], o2f(S.bmax[a][b][k]));
-        }
-      }
-      if (nl > 0 && nr > 0) {
-        float cost = box_area(l[0], l[1], l[2], l[3], l[4], l[5]) * nl + box_area(r[0], r[1], r[2], r[3], r[4], r[5]) * nr;
-        if (cost < bc) { bc = cost; bi = a * (NB - 1) + s; }
+    float l[6] = {1e30f, 1e30f, 1e30f, -1e30f, -1e30f, -1e30f}, r[6] = {1e30f, 1e30f, 1e30f, -1e30f, -1e30f, -1e30f};
+    int nl = 0, nr = 0;
+    for (int b = 0; b < NB; ++b) {
+      int cnt = S.bcnt[a][b];
+      if (cnt == 0) continue;
+      const bool lb = b <= s;
+      if (lb) nl += cnt; else nr += cnt;
+      for (int q = 0; q < 3; ++q) {
+        const float mn = o2f(S.bmin[a][b][q]), mx = o2f(S.bmax[a][b][q]);
+        if (lb) { l[q] = fminf(l[q], mn); l[3 + q] = fmaxf(l[3 + q], mx); }
+        else { r[q] = fminf(r[q], mn); r[3 + q] = fmaxf(r[3 + q], mx); }
       }
     }
+    if (nl > 0 && nr > 0) {
+      float cost = box_area(l[0], l[1], l[2], l[3], l[4], l[5]) * nl + box_area(r[0], r[1], r[2], r[3], r[4], r[5]) * nr;
+      if (cost < bc) { bc = cost; bi = k; }
+    }
   }
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oc = __shfl_xor_sync(FULL, bc, o);
+    const int oi = __shfl_xor_sync(FULL, bi, o);
+    if (oi >= 0 && (oc < bc || (oc == bc && (bi < 0 || oi < bi)))) { bc = oc; bi = oi; }
+  }
+  if (lane != 0) return;
+  nd.lo[0] = box[0]; nd.lo[1] = box[1]; nd.lo[2] = box[2];
+  nd.hi[0] = box[6]; nd.hi[1] = box[7]; nd.hi[2] = box[8];
   uint32_t nleft = t.count / 2;  // median split when no plane separates the centroids
   if (bi >= 0) {
     const int a = bi / (NB - 1), s = bi % (NB - 1);
@@ -464,7 +798,7 @@ __global__ void k_large_split(const BuildTask* large, uint32_t nlarge, LargeStat
   nd.right = (int32_t)(c + 1);
   nd.start = 0;
   nd.count = 0;
-  push_children(c, t, nleft, next_tasks, next_count, next_large, next_large_count, large_min);
+  push_children(c, t, nleft, next);
 }
 
 __device__ __forceinline__ bool large_goes_left(const LargeState& S, float4 c, int a, int s) {
@@ -698,7 +1032,7 @@ int build_bvh(const float4* tri_v0, const float4* tri_e1, const float4* tri_e2, 
   if (n == 0) return 0;
   Tmp<float4> tlo, thi, tc;
   Tmp<uint32_t> ids_a, ids_b, final_ids, counters, first_chunk, chunk_left;
-  Tmp<BuildTask> tasks_a, tasks_b, large_a, large_b;
+  Tmp<BuildTask> tasks_a, tasks_b, large_a, large_b, sub;
   Tmp<BuildNode> nodes;
   Tmp<LargeState> lstate;
   const uint32_t cap = 2 * n;
@@ -706,16 +1040,20 @@ int build_bvh(const float4* tri_v0, const float4* tri_e1, const float4* tri_e2, 
   if (tlo.alloc(n, st) || thi.alloc(n, st) || tc.alloc(n, st) || ids_a.alloc(n, st) || ids_b.alloc(n, st) ||
       final_ids.alloc(n, st) || counters.alloc(8, st) || tasks_a.alloc(n + 1, st) || tasks_b.alloc(n + 1, st) ||
       nodes.alloc(cap, st) || large_a.alloc(MAX_LARGE, st) || large_b.alloc(MAX_LARGE, st) ||
-      lstate.alloc(MAX_LARGE, st) || first_chunk.alloc(MAX_LARGE + 1, st) || chunk_left.alloc(max_chunks, st))
+      lstate.alloc(MAX_LARGE, st) || first_chunk.alloc(MAX_LARGE + 1, st) || chunk_left.alloc(max_chunks, st) ||
+      sub.alloc(n + 1, st))
     return 2;
   k_prep<<<(n + 255) / 256, 256, 0, st>>>(tri_v0, tri_e1, tri_e2, n, tlo.p, thi.p, tc.p, ids_a.p);
-  // counters: [0] node counter, [1]/[2] small-task counts A/B, [3]/[4] large-task counts A/B
+  // counters: [0] node counter, [1]/[2] small-task counts A/B, [3]/[4] large-task counts A/B,
+  // [5] whole-subtree tasks, [6] subtree error flag
   const BuildTask root{0, 0, n, 0};
+  const bool root_sub = n <= SUBTREE_MAX;
   const bool root_large = n > LARGE_TASK;
-  uint32_t init[8] = {1, root_large ? 0u : 1u, 0, root_large ? 1u : 0u, 0, 0, 0, 0};
-  cudaMemcpyAsync(root_large ? large_a.p : tasks_a.p, &root, sizeof(root), cudaMemcpyHostToDevice, st);
+  uint32_t init[8] = {1, (root_large || root_sub) ? 0u : 1u, 0, root_large ? 1u : 0u, 0, root_sub ? 1u : 0u, 0, 0};
+  cudaMemcpyAsync(root_sub ? sub.p : (root_large ? large_a.p : tasks_a.p), &root, sizeof(root), cudaMemcpyHostToDevice,
+                  st);
   cudaMemcpyAsync(counters.p, init, sizeof(init), cudaMemcpyHostToDevice, st);
-  uint32_t ntasks = root_large ? 0 : 1, nlarge = root_large ? 1 : 0;
+  uint32_t ntasks = (root_large || root_sub) ? 0 : 1, nlarge = root_large ? 1 : 0;
   std::vector<BuildTask> hlarge(MAX_LARGE);
   hlarge[0] = root;
   std::vector<uint32_t> hfirst(MAX_LARGE + 1);
@@ -730,10 +1068,20 @@ int build_bvh(const float4* tri_v0, const float4* tri_e1, const float4* tri_e2, 
   for (int level = 0; level < 200 && (ntasks > 0 || nlarge > 0); ++level) {
     cudaMemsetAsync(counters.p + nxt_slot, 0, sizeof(uint32_t), st);
     cudaMemsetAsync(counters.p + nxt_slot + 2, 0, sizeof(uint32_t), st);
+    ChildLists next;
+    next.tasks = nxt;
+    next.count = counters.p + nxt_slot;
+    next.large = lnxt;
+    next.large_count = counters.p + nxt_slot + 2;
+    next.large_min = LARGE_TASK;
+    next.sub = sub.p;
+    next.sub_count = counters.p + 5;
+    next.sub_max = SUBTREE_MAX;
+    next.sub_cap = n + 1;
+    next.dst_parity = dst == ids_b.p ? 1u : 0u;
     if (ntasks > 0)
       k_level<<<ntasks, BUILD_THREADS, 0, st>>>(cur, counters.p + cur_slot, src, dst, final_ids.p, tlo.p, thi.p,
-                                                tc.p, nodes.p, counters.p, nxt, counters.p + nxt_slot, lnxt,
-                                                counters.p + nxt_slot + 2, LARGE_TASK);
+                                                tc.p, nodes.p, counters.p, next);
     if (nlarge > 0) {
       uint32_t nchunks = 0;
       for (uint32_t j = 0; j < nlarge; ++j) {
@@ -747,9 +1095,7 @@ int build_bvh(const float4* tri_v0, const float4* tri_e1, const float4* tri_e2, 
       k_large_bounds<<<nchunks, BUILD_THREADS, 0, st>>>(lcur, first_chunk.p, nlarge, src, tlo.p, thi.p, tc.p,
                                                         lstate.p);
       k_large_bin<<<nchunks, BUILD_THREADS, 0, st>>>(lcur, first_chunk.p, nlarge, src, tlo.p, thi.p, tc.p, lstate.p);
-      k_large_split<<<(nlarge + 63) / 64, 64, 0, st>>>(lcur, nlarge, lstate.p, nodes.p, counters.p, nxt,
-                                                       counters.p + nxt_slot, lnxt, counters.p + nxt_slot + 2,
-                                                       LARGE_TASK);
+      k_large_split<<<(nlarge + 1) / 2, 64, 0, st>>>(lcur, nlarge, lstate.p, nodes.p, counters.p, next);
       k_large_count<<<nchunks, BUILD_THREADS, 0, st>>>(lcur, first_chunk.p, nlarge, src, tc.p, lstate.p,
                                                        chunk_left.p);
       k_large_scatter<<<nchunks, BUILD_THREADS, 0, st>>>(lcur, first_chunk.p, nlarge, src, dst, tc.p, lstate.p,
@@ -766,9 +1112,21 @@ int build_bvh(const float4* tri_v0, const float4* tri_e1, const float4* tri_e2, 
     std::swap(cur_slot, nxt_slot);
   }
   if (ntasks != 0 || nlarge != 0) return 4;
-  uint32_t nn = 0;
-  cudaMemcpyAsync(&nn, counters.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+  // the whole subtrees, one warp each, in one launch
+  cudaMemcpyAsync(host_counts, counters.p, sizeof(host_counts), cudaMemcpyDeviceToHost, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return 3;
+  const uint32_t nsub = std::min(host_counts[5], n + 1);
+  if (nsub > 0 &&
+      cudaFuncSetAttribute(k_subtree, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SUBTREE_SMEM) != cudaSuccess)
+    return 3;
+  if (nsub > 0)
+    k_subtree<<<(nsub + SUB_WARPS - 1) / SUB_WARPS, SUB_WARPS * 32, SUBTREE_SMEM, st>>>(
+        sub.p, counters.p + 5, n + 1, ids_a.p, ids_b.p, final_ids.p, tlo.p, thi.p, tc.p, nodes.p, counters.p,
+        counters.p + 6);
+  cudaMemcpyAsync(host_counts, counters.p, sizeof(host_counts), cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return 3;
+  if (host_counts[6] != 0) return 7;
+  const uint32_t nn = host_counts[0];
   if (nn > out.node_capacity) return 5;
   k_layout<<<(nn + 255) / 256, 256, 0, st>>>(nodes.p, nn, out.nodes);
   k_reorder<<<(n + 255) / 256, 256, 0, st>>>(final_ids.p, n, tri_v0, tri_e1, tri_e2, out.tri_sorted);
@@ -925,8 +1283,11 @@ extern "C" pt_status pt_bvh_build_noalloc(const void* tri_v0, const void* tri_e1
   uint32_t host_count = 0;
   for (int level = 0; level < 200 && ntasks > 0; ++level) {
     cudaMemsetAsync(counters + nxt_slot, 0, sizeof(uint32_t), st);
+    ChildLists next;
+    next.tasks = nxt;
+    next.count = counters + nxt_slot;
     k_level<<<ntasks, BUILD_THREADS, 0, st>>>(cur, counters + cur_slot, src, dst, final_ids, tlo, thi, tc, nodes,
-                                              counters, nxt, counters + nxt_slot);
+                                              counters, next);
     cudaMemcpyAsync(&host_count, counters + nxt_slot, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
     e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return na_fail(error_message, error_capacity, PT_ERR_CUDA, cudaGetErrorString(e));

@@ -134,6 +134,10 @@ struct pt_renderer {
   cudaStream_t stream = nullptr;
   std::string err;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // second stream of the commit: the environment's alias tables are built on
+  // it while the BVH builds on `stream`
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   uint32_t* pinned = nullptr;
 
   // scene

@@ -62,6 +62,8 @@ void launch_flatten(const float* raw_verts, const uint32_t* raw_idx, const PrimU
                     float4* tri_e2, uint32_t* tri_vidx, uint32_t* tri_mat, cudaStream_t st);
 // FP64 alias tables of the environment map; returns the FP64 luminance sum
 // through *total_out (device pointer to one double).
+// RGB float triples -> RGBA (alpha 0) environment texels.
+void launch_env_widen(const float* rgb, float4* env, size_t n, cudaStream_t st);
 void launch_env_tables(const float4* env, uint32_t w, uint32_t h, uint2* rows, uint2* cols, double* scratch_q,
                        uint32_t* scratch_stack, double* row_sums, double* total_out, cudaStream_t st);
 

@@ -2,6 +2,8 @@
 // mesh primitives and the FP64 alias tables of the environment map.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "pt_internal.h"
 
 namespace hpt {
@@ -122,6 +124,90 @@ __global__ void k_env_marginal(const double* row_sums, uint32_t h, double* q, ui
   vose(row_sums, h, q, stacks, stacks + h, rows);
 }
 
+// The same tables with one warp per row and the row in shared memory: lane 0
+// performs every order-dependent step (the sums and Vose's pairing loop) in
+// the order the sequential version does, the warp does the per-element steps
+// (luminance, q = w * n / total, the stable split into the small and large
+// lists, the final writes), so the tables are bit-identical and the
+// sequential part runs at shared-memory instead of L2 latency.
+__device__ void vose_warp(double* q, uint32_t n, double total, uint32_t* small, uint32_t* large, uint2* out) {
+  const unsigned FULL = 0xffffffffu;
+  const uint32_t lane = threadIdx.x & 31u;
+  if (!(total > 0.0)) {
+    for (uint32_t i = lane; i < n; i += 32) out[i] = make_uint2(__float_as_uint(1.0f), i);
+    return;
+  }
+  const unsigned lt = (1u << lane) - 1u;
+  uint32_t ns = 0, nl = 0;
+  for (uint32_t base = 0; base < n; base += 32) {
+    const uint32_t i = base + lane;
+    const bool v = i < n;
+    bool sm = false;
+    if (v) {
+      const double qi = __ddiv_rn(__dmul_rn(q[i], (double)n), total);
+      q[i] = qi;
+      sm = qi < 1.0;
+    }
+    const unsigned ms = __ballot_sync(FULL, v && sm), ml = __ballot_sync(FULL, v && !sm);
+    if (v) {
+      if (sm) small[ns + __popc(ms & lt)] = i;
+      else large[nl + __popc(ml & lt)] = i;
+    }
+    ns += __popc(ms);
+    nl += __popc(ml);
+  }
+  __syncwarp();
+  if (lane == 0) {
+    while (ns > 0 && nl > 0) {
+      uint32_t s = small[--ns];
+      uint32_t l = large[--nl];
+      out[s] = make_uint2(__float_as_uint((float)q[s]), l);
+      q[l] = __dsub_rn(__dadd_rn(q[l], q[s]), 1.0);
+      if (q[l] < 1.0) small[ns++] = l;
+      else large[nl++] = l;
+    }
+    while (nl > 0) { uint32_t l = large[--nl]; out[l] = make_uint2(__float_as_uint(1.0f), l); }
+    while (ns > 0) { uint32_t s = small[--ns]; out[s] = make_uint2(__float_as_uint(1.0f), s); }
+  }
+  __syncwarp();
+}
+
+// Shared memory of a row of n texels: q (n doubles), then the two stacks.
+__host__ __device__ inline size_t vose_smem(uint32_t n) { return (size_t)n * (sizeof(double) + 2 * sizeof(uint32_t)); }
+
+__global__ void __launch_bounds__(32) k_env_rows_warp(const float4* env, uint32_t w, double* row_sums, uint2* cols) {
+  extern __shared__ double sq[];
+  uint32_t* small = reinterpret_cast<uint32_t*>(sq + w);
+  uint32_t* large = small + w;
+  const uint32_t y = blockIdx.x, lane = threadIdx.x;
+  for (uint32_t x = lane; x < w; x += 32) sq[x] = lum64(env[(size_t)y * w + x]);
+  __syncwarp();
+  double rs = 0.0;
+  if (lane == 0) {
+    for (uint32_t x = 0; x < w; ++x) rs = __dadd_rn(rs, sq[x]);
+    row_sums[y] = rs;
+  }
+  rs = __shfl_sync(0xffffffffu, rs, 0);
+  vose_warp(sq, w, rs, small, large, cols + (size_t)y * w);
+}
+
+__global__ void __launch_bounds__(32) k_env_marginal_warp(const double* row_sums, uint32_t h, uint2* rows,
+                                                          double* total_out) {
+  extern __shared__ double sq[];
+  uint32_t* small = reinterpret_cast<uint32_t*>(sq + h);
+  uint32_t* large = small + h;
+  const uint32_t lane = threadIdx.x;
+  for (uint32_t y = lane; y < h; y += 32) sq[y] = row_sums[y];
+  __syncwarp();
+  double total = 0.0;
+  if (lane == 0) {
+    for (uint32_t y = 0; y < h; ++y) total = __dadd_rn(total, sq[y]);
+    *total_out = total;
+  }
+  total = __shfl_sync(0xffffffffu, total, 0);
+  vose_warp(sq, h, total, small, large, rows);
+}
+
 }  // namespace
 
 void launch_flatten(const float* raw_verts, const uint32_t* raw_idx, const PrimUpload* prims, uint32_t nprims,
@@ -136,13 +222,41 @@ void launch_flatten(const float* raw_verts, const uint32_t* raw_idx, const PrimU
                                                               tri_e1, tri_e2, tri_vidx, tri_mat);
 }
 
+__global__ void k_env_widen(const float* __restrict__ rgb, float4* __restrict__ env, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    env[i] = make_float4(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2], 0.0f);
+}
+
+void launch_env_widen(const float* rgb, float4* env, size_t n, cudaStream_t st) {
+  const size_t blocks = std::min<size_t>((n + 255) / 256, 65535);
+  k_env_widen<<<(unsigned)std::max<size_t>(blocks, 1), 256, 0, st>>>(rgb, env, n);
+}
+
 void launch_env_tables(const float4* env, uint32_t w, uint32_t h, uint2* rows, uint2* cols, double* scratch_q,
                        uint32_t* scratch_stack, double* row_sums, double* total_out, cudaStream_t st) {
   // scratch_q holds w*h weights followed by w*h working q values
   double* weights = scratch_q;
   double* q = scratch_q + (size_t)w * h;
-  k_env_rows<<<(h + 63) / 64, 64, 0, st>>>(env, w, h, weights, q, scratch_stack, row_sums, cols);
-  k_env_marginal<<<1, 1, 0, st>>>(row_sums, h, q, scratch_stack, rows, total_out);
+  int dev = 0, smem_max = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const size_t row_smem = vose_smem(w), marg_smem = vose_smem(h);
+  if (row_smem <= (size_t)smem_max &&
+      cudaFuncSetAttribute(k_env_rows_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)row_smem) ==
+          cudaSuccess) {
+    k_env_rows_warp<<<h, 32, row_smem, st>>>(env, w, row_sums, cols);
+  } else {
+    cudaGetLastError();
+    k_env_rows<<<(h + 63) / 64, 64, 0, st>>>(env, w, h, weights, q, scratch_stack, row_sums, cols);
+  }
+  if (marg_smem <= (size_t)smem_max &&
+      cudaFuncSetAttribute(k_env_marginal_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)marg_smem) ==
+          cudaSuccess) {
+    k_env_marginal_warp<<<1, 32, marg_smem, st>>>(row_sums, h, rows, total_out);
+  } else {
+    cudaGetLastError();
+    k_env_marginal<<<1, 1, 0, st>>>(row_sums, h, q, scratch_stack, rows, total_out);
+  }
 }
 
 }  // namespace hpt

@@ -81,6 +81,23 @@ def test_bvh_axis_aligned_rays(pt, scenes, oracle_mod, name):
     assert np.array_equal(r.trace_rays(rays, any_hit=True)[:, 3], o.trace_rays(rays, any_hit=True)[:, 3])
 
 
+@pytest.mark.parametrize("freq", [16, 72])
+def test_bvh_large_scene_bitexact(pt, scenes, freq):
+    """Scenes that take every build path: 5,122 triangles (one-block levels
+    and whole subtrees) and 103,682 (also the multi-block top levels).
+    Closest hits and any-hit answers equal brute force over all triangles."""
+    sc = scenes.displaced_icosphere(64, 36, 1, freq=freq)
+    sc.lights = []
+    r = pt.renderer_for(sc)
+    assert r.stats().triangles == 20 * freq * freq + 2
+    rays = _random_rays(_bounds(sc), 4000, 13)
+    assert np.array_equal(r.trace_rays(rays), r.trace_rays(rays, brute_force=True))
+    rays[:, 7] = np.random.default_rng(4).uniform(0.01, 1.0, len(rays))
+    a = r.trace_rays(rays, any_hit=True)
+    b = r.trace_rays(rays, any_hit=True, brute_force=True)
+    assert np.array_equal(a[:, 3], b[:, 3])
+
+
 @pytest.mark.parametrize("name", ["cornell", "icosphere"])
 def test_bvh_any_hit(pt, scenes, oracle_mod, name):
     sc = scenes.tiny_variants()[name]
