@@ -98,6 +98,37 @@ def test_bvh_large_scene_bitexact(pt, scenes, freq):
     assert np.array_equal(a[:, 3], b[:, 3])
 
 
+def test_bvh_degenerate_geometry(pt, scenes):
+    """Inputs where no SAH plane separates the centroids, so every build tier
+    falls back to median splits: 20,000 copies of one triangle (multi-block,
+    one-block and whole-subtree tasks), 3,000 triangles in one plane, 600
+    triangles sharing a centroid. Closest hits (equal distances resolved by
+    the lower id) and any-hit answers equal brute force."""
+    sc = scenes.tiny_variants()["cornell"]
+    sc.meshes = []
+    sc.lights = []
+    mat = sc.add_material(scenes.material())
+    rng = np.random.default_rng(17)
+    tri = np.array([[0.2, 0.2, 0.3], [0.8, 0.3, 0.4], [0.4, 0.9, 0.6]])
+    z = np.zeros((3, 3))
+    sc.add_mesh(scenes.pack_vertices(tri, z, z, np.zeros((3, 2))), np.tile(np.arange(3, dtype=np.uint32), 20000), mat)
+    flat = rng.uniform(0, 1, size=(9000, 3))
+    flat[:, 2] = 0.5
+    n = np.zeros((9000, 3))
+    sc.add_mesh(scenes.pack_vertices(flat, n, n, np.zeros((9000, 2))), np.arange(9000, dtype=np.uint32), mat)
+    c = np.array([0.5, 0.5, 0.5])
+    nested = np.concatenate([c + s * (tri - tri.mean(0)) for s in np.linspace(0.05, 1.5, 600)])
+    n = np.zeros((1800, 3))
+    sc.add_mesh(scenes.pack_vertices(nested, n, n, np.zeros((1800, 2))), np.arange(1800, dtype=np.uint32), mat)
+    r = pt.renderer_for(sc)
+    assert r.stats().triangles == 23600
+    rays = _random_rays((np.zeros(3), np.ones(3)), 4000, 23)
+    assert np.array_equal(r.trace_rays(rays), r.trace_rays(rays, brute_force=True))
+    rays[:, 7] = rng.uniform(0.01, 1.0, len(rays))
+    assert np.array_equal(r.trace_rays(rays, any_hit=True)[:, 3],
+                          r.trace_rays(rays, any_hit=True, brute_force=True)[:, 3])
+
+
 @pytest.mark.parametrize("name", ["cornell", "icosphere"])
 def test_bvh_any_hit(pt, scenes, oracle_mod, name):
     sc = scenes.tiny_variants()[name]
