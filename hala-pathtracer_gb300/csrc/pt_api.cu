@@ -65,6 +65,7 @@ cudaError_t WaveBuffers::ensure(uint32_t want, bool want_med, bool want_multi) {
   chk(q_logic.ensure(want));
   chk(q_diff.ensure(want));
   chk(q_dis.ensure(want));
+  chk(q_glass.ensure(want));
   chk(q_shadow.ensure(want));
   chk(counters.ensure(2 * Q_COUNT + G_WORDS));
   chk(rays.ensure(4));
@@ -96,8 +97,8 @@ cudaError_t WaveBuffers::ensure(uint32_t want, bool want_med, bool want_multi) {
 
 uint64_t WaveBuffers::bytes_per_path(bool med, bool multi) {
   // rng 16, ray_o/ray_d/hit/thr/rad/albedo/normal 7x16, depth+flags 8,
-  // six NEE float4 96, six queues 24 (+ medium 24, + job slot 4)
-  return 16 + 7 * 16 + 8 + 96 + 24 + (med ? 24 : 0) + (multi ? 4 : 0);
+  // six NEE float4 96, seven queues 28 (+ medium 24, + job slot 4)
+  return 16 + 7 * 16 + 8 + 96 + 28 + (med ? 24 : 0) + (multi ? 4 : 0);
 }
 
 cudaError_t run_bounces(const DevScene& S, WaveBuffers& W, uint32_t live, uint32_t max_depth, BounceLoop& L,
@@ -105,7 +106,7 @@ cudaError_t run_bounces(const DevScene& S, WaveBuffers& W, uint32_t live, uint32
   uint32_t* cnt0 = W.counters.p;
   uint32_t* cnt1 = W.counters.p + Q_COUNT;
   const uint32_t bounce_cap = 4u * max_depth + 4096u;
-  const uint64_t per_bounce = (S.features & PT_FEATURE_MEDIUM) ? 4 : 5;  // trace, logic, 2 shades (, shadow)
+  const uint64_t per_bounce = (S.features & PT_FEATURE_MEDIUM) ? 5 : 6;  // trace, logic, 3 shades (, shadow)
   if (live == 0) {
     L.bounces = 0;
     L.timed_out = false;
@@ -122,7 +123,8 @@ cudaError_t run_bounces(const DevScene& S, WaveBuffers& W, uint32_t live, uint32
     uint32_t* qnext = (b & 1) ? W.q_a.p : W.q_b.p;
     cudaError_t e = cudaMemsetAsync(out, 0, Q_COUNT * sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
-    QueueSet Q{qin, in_cnt, qnext, W.q_logic.p, W.q_diff.p, W.q_dis.p, W.q_shadow.p, out, W.rays.p};
+    QueueSet Q{qin, in_cnt, qnext, W.q_logic.p, W.q_diff.p, W.q_dis.p, W.q_glass.p, W.q_shadow.p, out,
+                 W.rays.p};
     if (timing) {
       while (L.tev->size() < 2 * (L.ntimed + 1)) {
         cudaEvent_t ev;
@@ -216,6 +218,7 @@ void renderer_drop_scene(pt_renderer* r) {
   r->tri_vidx.release();
   r->tri_mat.release();
   r->dmats.release();
+  r->dmat_class.release();
   r->env.release();
   r->alias_rows.release();
   r->alias_cols.release();
@@ -285,6 +288,18 @@ void normal_matrix(const float* T, float N[9]) {
   for (int i = 0; i < 9; ++i) N[i] = C[i] / det;
 }
 
+// Shading kernel of a material (MAT_CLASS_*). The glass lobe's weight is
+// (1 - metallic) * specular_transmission, computed as the lobe probabilities
+// compute it; a metallic-roughness map replaces metallic per hit, so there
+// only a zero transmission rules the lobe out.
+uint32_t material_class(const pt_material& m, uint32_t num_textures) {
+  if (m.type != PT_MATERIAL_DISNEY) return MAT_CLASS_DIFFUSE;
+  if (m.specular_transmission == 0.0f) return MAT_CLASS_DISNEY;
+  if (m.metallic_roughness_map_index < num_textures) return MAT_CLASS_GLASS;
+  const float glass_wt = (1.0f - m.metallic) * m.specular_transmission;
+  return glass_wt > 0.0f ? MAT_CLASS_GLASS : MAT_CLASS_DISNEY;
+}
+
 void fill_view(pt_renderer* r) {
   DevScene& S = r->view;
   S = DevScene{};
@@ -296,6 +311,7 @@ void fill_view(pt_renderer* r) {
   S.vtan = r->vtan.p;
   S.vuv = r->vuv.p;
   S.mats = r->dmats.p;
+  S.mat_class = r->dmat_class.p;
   S.num_mats = (uint32_t)r->mats.size();
   S.num_tris = r->ntris;
   S.num_lights = (uint32_t)r->lights.size();
@@ -604,6 +620,14 @@ pt_status pt_renderer_set_scene(pt_renderer* r, const pt_scene_desc* s) {
   CK(r, r->tri_vidx.ensure(3 * T));
   CK(r, r->tri_mat.ensure(T));
   CK(r, r->dmats.ensure(std::max<size_t>(r->mats.size(), 1)));
+  {
+    std::vector<uint32_t>& cls = r->mat_class;
+    cls.resize(r->mats.size());
+    for (size_t i = 0; i < r->mats.size(); ++i) cls[i] = material_class(r->mats[i], s->num_textures);
+    CK(r, r->dmat_class.ensure(std::max<size_t>(cls.size(), 1)));
+    if (!cls.empty())
+      CK(r, cudaMemcpyAsync(r->dmat_class.p, cls.data(), cls.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+  }
   if (!r->mats.empty())
     CK(r, cudaMemcpyAsync(r->dmats.p, r->mats.data(), r->mats.size() * sizeof(pt_material), cudaMemcpyHostToDevice,
                           st));

@@ -585,6 +585,9 @@ __device__ __forceinline__ LobeProbs lobe_probs(const pt_material& m, float eta,
 }
 
 // disney.glsl:264-390 (ROUGHNESS_REGULARIZE_EVAL)
+// GLASS = false leaves out the glass lobe, for materials whose glass weight
+// is zero: its branches are then never taken, so the result is the same.
+template <bool GLASS>
 static __device__ __noinline__ float3 disney_eval(bool ans, const ShadeFrame& s, const pt_material& m, float3 V,
                                            float3 N, float3 L, float& pdf) {
   float ax = m.ax, ay = m.ay;
@@ -621,7 +624,7 @@ static __device__ __noinline__ float3 disney_eval(bool ans, const ShadeFrame& s,
     f += eval_microfacet_ms(ax, ay, V, L, base) * p.metal_wt;
     pdf += tmp * p.metal_pr;
   }
-  if (p.glass_pr > 0.0f) {
+  if (GLASS && p.glass_pr > 0.0f) {
     float F = dielectric_fresnel(vdh, s.eta);
     if (refl) {
       f += eval_microfacet_reflection(ax, ay, V, L, H, f3(F), tmp) * p.glass_wt;
@@ -639,7 +642,8 @@ static __device__ __noinline__ float3 disney_eval(bool ans, const ShadeFrame& s,
   return f * fabsf(L.z);
 }
 
-// disney.glsl:405-531
+// disney.glsl:405-531 (GLASS as for disney_eval)
+template <bool GLASS>
 __device__ __forceinline__ float3 disney_sample(uint4& rng, bool& ans, const ShadeFrame& s, const pt_material& m,
                                                 float3 V, float3 N, float3& L, float& pdf, uint32_t& flags) {
   float ax = m.ax, ay = m.ay;
@@ -663,7 +667,7 @@ __device__ __forceinline__ float3 disney_sample(uint4& rng, bool& ans, const Sha
     if (H.z < 0.0f) H = -H;
     L = normalize(reflect3(-V, H));
     flags = RAY_FLAGS_REFLECTION | (1u << 8);
-  } else if (r3 < cdf3) {
+  } else if (GLASS && r3 < cdf3) {
     float3 H = sample_ggx_vndf(V, ax, ay, r1, r2);
     float F = dielectric_fresnel(fabsf(dot(V, H)), s.eta);
     if (H.z < 0.0f) H = -H;
@@ -683,19 +687,21 @@ __device__ __forceinline__ float3 disney_sample(uint4& rng, bool& ans, const Sha
   }
   L = to_world(s.tangent, s.bitangent, N, L);
   V = to_world(s.tangent, s.bitangent, N, V);
-  return disney_eval(ans, s, m, V, N, L, pdf);
+  return disney_eval<GLASS>(ans, s, m, V, N, L, pdf);
 }
 
 template <int MAT>
 __device__ __forceinline__ float3 bsdf_eval(const ShadeFrame& s, const pt_material& m, bool ans, float3 V, float3 N,
                                             float3 L, float& pdf) {
-  if (MAT == PT_MATERIAL_DISNEY) return disney_eval(ans, s, m, V, N, L, pdf);
+  if (MAT == SHADE_DISNEY_GLASS) return disney_eval<true>(ans, s, m, V, N, L, pdf);
+  if (MAT == PT_MATERIAL_DISNEY) return disney_eval<false>(ans, s, m, V, N, L, pdf);
   return diffuse_eval(s, m, V, N, L, pdf);
 }
 template <int MAT>
 __device__ __forceinline__ float3 bsdf_sample(uint4& rng, bool& ans, const ShadeFrame& s, const pt_material& m,
                                               float3 V, float3 N, float3& L, float& pdf, uint32_t& flags) {
-  if (MAT == PT_MATERIAL_DISNEY) return disney_sample(rng, ans, s, m, V, N, L, pdf, flags);
+  if (MAT == SHADE_DISNEY_GLASS) return disney_sample<true>(rng, ans, s, m, V, N, L, pdf, flags);
+  if (MAT == PT_MATERIAL_DISNEY) return disney_sample<false>(rng, ans, s, m, V, N, L, pdf, flags);
   return diffuse_sample(rng, ans, s, m, V, N, L, pdf, flags);
 }
 

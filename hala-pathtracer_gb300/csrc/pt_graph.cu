@@ -6,7 +6,7 @@
 //          }
 //
 // A bounce is the same kernel sequence the host-driven loop launches
-// (closest hit, surface logic, the two material kernels, shadow rays); the
+// (closest hit, surface logic, the three material kernels, shadow rays); the
 // bounce kernels read their queue lengths from device memory, so a grid at
 // least as large as the queue gives the same result as an exact one. The
 // one-thread control kernels read the continuing-path count, clear the
@@ -86,7 +86,8 @@ QueueSet queues_for(WaveBuffers& W, uint32_t parity) {
   uint32_t* in_cnt = (parity ? cnt0 : cnt1) + Q_NEXT;
   uint32_t* qin = parity ? W.q_b.p : W.q_a.p;
   uint32_t* qnext = parity ? W.q_a.p : W.q_b.p;
-  return QueueSet{qin, in_cnt, qnext, W.q_logic.p, W.q_diff.p, W.q_dis.p, W.q_shadow.p, out, W.rays.p};
+  return QueueSet{qin, in_cnt, qnext, W.q_logic.p, W.q_diff.p, W.q_dis.p, W.q_glass.p, W.q_shadow.p, out,
+                  W.rays.p};
 }
 
 void append(std::vector<unsigned char>& k, const void* p, size_t n) {
@@ -237,7 +238,7 @@ cudaError_t run_bounces_graph(const DevScene& S, WaveBuffers& W, uint32_t bounce
     return e;
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
   const uint32_t done = pinned[G_DONE], live = pinned[G_LIVE];
-  const uint64_t per_bounce = (S.features & PT_FEATURE_MEDIUM) ? 4 : 5;
+  const uint64_t per_bounce = (S.features & PT_FEATURE_MEDIUM) ? 5 : 6;
   L.bounces = done;
   L.timed_out = live > 0;
   L.launches = per_bounce * done + 1 + 2ull * ((done + 1) / 2);  // bounces, init, two control kernels per iteration

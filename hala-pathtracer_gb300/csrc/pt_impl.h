@@ -92,7 +92,7 @@ struct WaveBuffers {
   Buf<float2> med1;
   Buf<float4> sh_o, sh_d0, sh_d1, sh_c0, sh_c1, sh_T;
   Buf<uint32_t> depth, flags, job;
-  Buf<uint32_t> q_a, q_b, q_logic, q_diff, q_dis, q_shadow, counters;
+  Buf<uint32_t> q_a, q_b, q_logic, q_diff, q_dis, q_glass, q_shadow, counters;
   Buf<unsigned long long> rays;
   PathState P{};
   BounceGraph graph;
@@ -154,6 +154,8 @@ struct pt_renderer {
   hpt::Buf<float2> vuv;
   hpt::Buf<uint32_t> tri_vidx, tri_mat;
   hpt::Buf<pt_material> dmats;
+  hpt::Buf<uint32_t> dmat_class;
+  std::vector<uint32_t> mat_class;  // host copy (kept alive for the asynchronous upload)
   hpt::Buf<float4> tex_texels;
   hpt::Buf<uint4> tex_info;
   uint32_t num_textures = 0;

@@ -16,6 +16,7 @@ struct QueueSet {
   uint32_t* logic;
   uint32_t* diffuse;
   uint32_t* disney;
+  uint32_t* glass;
   uint32_t* shadow;
   uint32_t* counts;            // [Q_COUNT], zeroed at the start of the bounce
   unsigned long long* rays;    // [0] closest rays, [1] shadow rays, [2] nodes, [3] triangle tests

@@ -128,14 +128,15 @@ __global__ void __launch_bounds__(256, 5) k_trace(const __grid_constant__ DevSce
     float4 o4 = P.ray_o[p], d4 = P.ray_d[p];
     HitRec h = trace_closest<BRUTE, COUNT>(S, f3(o4), f3(d4), 0.0f, WORLD_SIZE, &tc);
     P.hit[p] = make_float4(h.t, h.u, h.v, __uint_as_float(h.id));
-    int cls = 0;  // 0 logic, 1 diffuse, 2 disney
+    uint32_t cls = 0;  // surface logic, else MAT_CLASS_*
     if (h.id != HIT_MISS && !(h.id & HIT_LIGHT_BIT)) {
       uint32_t m = __ldg(&S.tri_mat[h.id]);
-      if (m < S.num_mats) cls = (S.mats[m].type == PT_MATERIAL_DISNEY) ? 2 : 1;
+      if (m < S.num_mats) cls = __ldg(&S.mat_class[m]);
     }
     queue_push(Q.logic, &Q.counts[Q_LOGIC], p, cls == 0);
-    queue_push(Q.diffuse, &Q.counts[Q_DIFFUSE], p, cls == 1);
-    queue_push(Q.disney, &Q.counts[Q_DISNEY], p, cls == 2);
+    queue_push(Q.diffuse, &Q.counts[Q_DIFFUSE], p, cls == MAT_CLASS_DIFFUSE);
+    queue_push(Q.disney, &Q.counts[Q_DISNEY], p, cls == MAT_CLASS_DISNEY);
+    queue_push(Q.glass, &Q.counts[Q_GLASS], p, cls == MAT_CLASS_GLASS);
     count_add(&Q.rays[0], 1u);
   }
   if (COUNT) {

@@ -452,8 +452,8 @@ __device__ __forceinline__ void apply_maps(const DevScene& S, pt_material& m, Su
 
 template <int MAT, bool MEDIUM, bool TRANSPARENT, bool MULTI, bool CACHE = false, bool TEXTURED = false>
 __global__ void __launch_bounds__(256, MEDIUM ? 4 : 3) k_shade(const __grid_constant__ DevScene S0, PathState P, QueueSet Q) {
-  const int slot = MAT == PT_MATERIAL_DISNEY ? Q_DISNEY : Q_DIFFUSE;
-  const uint32_t* qin = MAT == PT_MATERIAL_DISNEY ? Q.disney : Q.diffuse;
+  const int slot = MAT == SHADE_DISNEY_GLASS ? Q_GLASS : (MAT == PT_MATERIAL_DISNEY ? Q_DISNEY : Q_DIFFUSE);
+  const uint32_t* qin = MAT == SHADE_DISNEY_GLASS ? Q.glass : (MAT == PT_MATERIAL_DISNEY ? Q.disney : Q.diffuse);
   const uint32_t n = Q.counts[slot];
   unsigned long long nshadow_total = 0;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {

@@ -10,6 +10,7 @@ template <bool MED, bool TR, bool TEX>
 void two(const DevScene& S, const PathState& P, const QueueSet& Q, int g, cudaStream_t st) {
   k_shade<PT_MATERIAL_DIFFUSE, MED, TR, true, false, TEX><<<g, 256, 0, st>>>(S, P, Q);
   k_shade<PT_MATERIAL_DISNEY, MED, TR, true, false, TEX><<<g, 256, 0, st>>>(S, P, Q);
+  k_shade<SHADE_DISNEY_GLASS, MED, TR, true, false, TEX><<<g, 256, 0, st>>>(S, P, Q);
 }
 
 template <bool MED, bool TR>

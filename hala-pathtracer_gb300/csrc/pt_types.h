@@ -73,6 +73,8 @@ struct DevScene {
   const float4* vtan;
   const float2* vuv;
   const pt_material* mats;
+  // per material, which shading kernel takes its hits: MAT_CLASS_*
+  const uint32_t* mat_class;
   uint32_t num_mats;
   uint32_t num_tris;
   uint32_t num_lights;
@@ -149,15 +151,24 @@ struct WaveSegment {
 constexpr uint32_t ANS_BIT = 0x100u;        // any_non_specular_bounce
 constexpr uint32_t IN_MEDIUM_BIT = 0x200u;  // is_in_medium
 
+// Shading kernel of a material (DevScene::mat_class; 0 = the surface-logic
+// kernel: misses, lights, invalid materials). A Disney material whose glass
+// lobe has zero weight, (1 - metallic) * specular_transmission as the lobe
+// probabilities compute it, is shaded by a kernel built without that lobe.
+constexpr uint32_t MAT_CLASS_DIFFUSE = 1, MAT_CLASS_DISNEY = 2, MAT_CLASS_GLASS = 3;
+// Template argument of k_shade for the glass-capable Disney kernel.
+constexpr int SHADE_DISNEY_GLASS = 2;
+
 // Queue counters (device memory)
 enum QueueSlot : int {
   Q_NEXT = 0,     // paths continuing to the next bounce
   Q_LOGIC = 1,    // miss / emitter / invalid-material hits
   Q_DIFFUSE = 2,  // surface hits on diffuse materials
-  Q_DISNEY = 3,   // surface hits on Disney materials
+  Q_DISNEY = 3,   // surface hits on Disney materials without a glass lobe
   Q_SHADOW = 4,   // paths with pending shadow rays
   C_CLOSEST = 5,  // closest-hit rays traced (64-bit pair: 5,6)
   C_SHADOW = 7,   // shadow/transmittance rays traced (64-bit pair: 7,8)
+  Q_GLASS = 9,    // surface hits on Disney materials whose glass lobe can be sampled
   Q_COUNT = 16
 };
 
