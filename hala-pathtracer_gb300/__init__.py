@@ -124,6 +124,17 @@ class Renderer:
     def reset(self):
         self._check(self._lib.pt_renderer_reset(self._h))
 
+    def load_accumulation(self, accum, albedo, normal, frame_index):
+        """Resumes from saved (H, W, 4) float32 accum / albedo / normal images
+        holding `frame_index` frames (image() and stats().frame_index of the
+        saved renderer); later frames continue bit-identically."""
+        imgs = [np.ascontiguousarray(a, np.float32) for a in (accum, albedo, normal)]
+        for a in imgs:
+            if a.shape != (self.height, self.width, 4):
+                raise ValueError(f"image shape {a.shape} != {(self.height, self.width, 4)}")
+        self._check(self._lib.pt_renderer_load_accumulation(self._h, *(a.ctypes.data for a in imgs),
+                                                            int(frame_index)))
+
     def wait_idle(self):
         self._check(self._lib.pt_renderer_wait_idle(self._h))
 

@@ -190,6 +190,7 @@ RENDERER_SIGNATURES = {
     "pt_renderer_commit": (C.c_int, [C.c_void_p]),
     "pt_renderer_render": (C.c_int, [C.c_void_p, C.c_uint32]),
     "pt_renderer_reset": (C.c_int, [C.c_void_p]),
+    "pt_renderer_load_accumulation": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64]),
     "pt_renderer_read_image": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t]),
     "pt_renderer_save_images": (C.c_int, [C.c_void_p, C.c_char_p]),
     "pt_renderer_wait_idle": (C.c_int, [C.c_void_p]),

@@ -980,6 +980,25 @@ pt_status pt_renderer_reset(pt_renderer* r) {
   return PT_OK;
 }
 
+pt_status pt_renderer_load_accumulation(pt_renderer* r, const float* accum, const float* albedo, const float* normal,
+                                        uint64_t frame_index) {
+  if (!r) return PT_ERR_INVALID_ARG;
+  if (!accum || !albedo || !normal) return fail(r, PT_ERR_INVALID_ARG, "image pointer is null");
+  if (r->cfg.max_samples > 0 && frame_index > r->cfg.max_samples)
+    return fail(r, PT_ERR_INVALID_ARG, "frame_index exceeds max_samples");
+  const size_t WH = (size_t)r->cfg.width * r->cfg.height;
+  CK(r, cudaMemcpyAsync(r->accum.p, accum, WH * sizeof(float4), cudaMemcpyHostToDevice, r->stream));
+  CK(r, cudaMemcpyAsync(r->albedo.p, albedo, WH * sizeof(float4), cudaMemcpyHostToDevice, r->stream));
+  CK(r, cudaMemcpyAsync(r->normal.p, normal, WH * sizeof(float4), cudaMemcpyHostToDevice, r->stream));
+  launch_finalize(r->accum.p, r->final_img.p, (uint32_t)WH, r->exposure, r->cfg.enable_tonemap, r->cfg.enable_aces,
+                  r->cfg.use_simple_aces, r->stream);
+  CK(r, cudaGetLastError());
+  CK(r, cudaStreamSynchronize(r->stream));
+  r->frame_index = frame_index;
+  r->stats.frame_index = frame_index;
+  return PT_OK;
+}
+
 pt_status pt_renderer_read_image(pt_renderer* r, pt_image which, void* host, size_t bytes) {
   if (!r) return PT_ERR_INVALID_ARG;
   if (!host) return fail(r, PT_ERR_INVALID_ARG, "host pointer is null");

@@ -262,6 +262,16 @@ pt_status pt_renderer_commit(pt_renderer* r);
 pt_status pt_renderer_render(pt_renderer* r, uint32_t frames);
 /* Restart accumulation at frame 0. */
 pt_status pt_renderer_reset(pt_renderer* r);
+/* Resumes a progressive render from saved accumulation: the accum, albedo
+ * and normal images as pt_renderer_read_image returns them (RGBA32F,
+ * width * height each) and the number of frames they hold
+ * (pt_stats.frame_index). The random sequence of a pixel depends only on the
+ * pixel and the frame, so frames rendered afterwards continue exactly where
+ * the saved render stopped: the result is bit-identical to an uninterrupted
+ * render. The final image is recomputed from accum. No counterpart in the
+ * reference, whose accumulation lives only in GPU images. */
+pt_status pt_renderer_load_accumulation(pt_renderer* r, const float* accum, const float* albedo,
+                                        const float* normal, uint64_t frame_index);
 /* Device->host copy of one image (the data HalaRenderer::save_images writes,
  * src/bin/hala-pathtracer.rs:251). `bytes` must equal the image size. */
 pt_status pt_renderer_read_image(pt_renderer* r, pt_image which, void* host, size_t bytes);

@@ -209,3 +209,25 @@ def test_gpu_matches_reference_golden(pt, name):
             assert np.array_equal(got, g[k]), f"{name}: final image differs"
         else:
             assert np.array_equal(got.view(np.uint32), g[k].view(np.uint32)), f"{name}: {k} differs"
+
+
+def test_converges_to_the_fp64_oracle(pt, scenes):
+    """The 128x128 Cornell box rendered on the GPU with an independent seed
+    against the oracle's 4096-spp FP64 image: the error falls as 1/sqrt(spp)
+    and the mean difference stays within its noise (no bias)."""
+    import os
+    ref = np.load(os.path.join(os.path.dirname(__file__), "golden", "cornell128_4096spp_fp64.npz"))
+    ref = ref["radiance"].astype(np.float64)
+    s = scenes.cornell(128, 128, 1024, max_depth=8, rr_depth=0, seed=1)
+    r = pt.renderer_for(s, seed=7)
+    err = {}
+    for total, step in ((64, 64), (256, 192), (1024, 768)):
+        r.render(step)
+        d = r.image(0)[..., :3].astype(np.float64) - ref
+        err[total] = float(np.sqrt((d ** 2).mean()))
+    assert 0.4 < err[256] / err[64] < 0.62, err
+    assert 0.4 < err[1024] / err[256] < 0.62, err
+    npix = d.shape[0] * d.shape[1]
+    for c in range(3):
+        dc = d[..., c].ravel()
+        assert abs(dc.mean()) < 5.0 * dc.std() / np.sqrt(npix), (c, dc.mean(), dc.std())

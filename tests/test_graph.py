@@ -42,3 +42,26 @@ def test_graph_progressive_frames(pt, abi, scenes):
     whole, _ = _render(pt, abi, sc, abi.PROFILE_HOST_LOOP, sc.spp)
     assert np.array_equal(per_frame[0].view(np.uint32), whole[0].view(np.uint32))
     assert np.array_equal(per_frame[1], whole[3])
+
+
+@pytest.mark.parametrize("name", ["cornell", "disney"])
+def test_resume_from_saved_accumulation(pt, abi, scenes, name):
+    """Checkpoint after some frames, resume in a new renderer, finish: the
+    images equal an uninterrupted render bit for bit."""
+    sc = scenes.tiny_variants()[name]
+    first = 3
+    a = pt.renderer_for(sc)
+    a.render(first)
+    saved = [a.image(w) for w in (abi.IMAGE_ACCUM, abi.IMAGE_ALBEDO, abi.IMAGE_NORMAL)]
+    frames = a.stats().frame_index
+    a.close()
+    assert frames == first
+    b = pt.renderer_for(sc)
+    b.load_accumulation(*saved, frames)
+    assert np.array_equal(b.image(abi.IMAGE_ACCUM).view(np.uint32), saved[0].view(np.uint32))
+    b.render(4)
+    whole = pt.renderer_for(sc)
+    whole.render(first + 4)
+    assert b.stats().frame_index == whole.stats().frame_index == first + 4
+    for w in (abi.IMAGE_ACCUM, abi.IMAGE_ALBEDO, abi.IMAGE_NORMAL, abi.IMAGE_FINAL):
+        assert np.array_equal(b.image(w).view(np.uint8), whole.image(w).view(np.uint8)), f"image {w} differs"
