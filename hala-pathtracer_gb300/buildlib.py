@@ -37,7 +37,8 @@ def headers():
 
 # Shading code is compiled without multiply-add contraction so it rounds like
 # the CPU oracle (explicit fmaf calls are still fused).
-PER_FILE_FLAGS = {f: ["-fmad=false"] for f in ("pt_render.cu", "pt_shade_single.cu", "pt_shade_multi.cu")}
+PER_FILE_FLAGS = {f: ["-fmad=false"] for f in ("pt_render.cu", "pt_shade_plain.cu", "pt_shade_medium.cu",
+                                                "pt_shade_cache.cu", "pt_shade_multi.cu", "pt_shade_multi_medium.cu")}
 
 
 def _compile(src, verbose_ptxas=False):

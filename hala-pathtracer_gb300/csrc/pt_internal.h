@@ -30,12 +30,20 @@ void launch_camera(const DevScene& S, const PathState& P, uint64_t g0, uint32_t 
 void launch_trace(const DevScene& S, const PathState& P, const QueueSet& Q, uint32_t max_items, bool count,
                   cudaStream_t st);
 void launch_shade(const DevScene& S, const PathState& P, const QueueSet& Q, uint32_t max_items, cudaStream_t st);
-// pt_shade_single.cu / pt_shade_multi.cu: the two material kernels of one
-// bounce (diffuse, Disney) in the variant the feature flags select.
-void launch_materials_single(const DevScene& S, const PathState& P, const QueueSet& Q, int grid, bool med, bool tr,
-                             bool tex, bool cache, cudaStream_t st);
-void launch_materials_multi(const DevScene& S, const PathState& P, const QueueSet& Q, int grid, bool med, bool tr,
-                            bool tex, cudaStream_t st);
+// pt_shade_*.cu: the three material kernels of one bounce (diffuse, opaque
+// Disney, glass Disney) for single-scene wavefronts without media
+// (plain), with media (medium), with a radiance cache (cache), and for
+// shared multi-job wavefronts without and with media.
+void launch_materials_plain(const DevScene& S, const PathState& P, const QueueSet& Q, int grid, bool tr, bool tex,
+                            cudaStream_t st);
+void launch_materials_medium(const DevScene& S, const PathState& P, const QueueSet& Q, int grid, bool tr, bool tex,
+                             cudaStream_t st);
+void launch_materials_cache(const DevScene& S, const PathState& P, const QueueSet& Q, int grid, bool tr, bool tex,
+                            cudaStream_t st);
+void launch_materials_multi(const DevScene& S, const PathState& P, const QueueSet& Q, int grid, bool tr, bool tex,
+                            cudaStream_t st);
+void launch_materials_multi_medium(const DevScene& S, const PathState& P, const QueueSet& Q, int grid, bool tr,
+                                   bool tex, cudaStream_t st);
 void launch_camera_multi(const PathState& P, const WaveSegment* segs, uint32_t nseg, uint32_t n, uint32_t* q_active,
                          uint32_t* active_count, cudaStream_t st);
 void launch_accumulate(const PathState& P, uint64_t g0, uint32_t n, uint32_t WH, float4* accum, float4* albedo,

@@ -299,11 +299,14 @@ void launch_shade(const DevScene& S, const PathState& P, const QueueSet& Q, uint
   const bool tex = (S.features & PT_FEATURE_TEXTURED) != 0;
   if (P.job) {
     k_shade_logic<true><<<g, 256, 0, st>>>(S, P, Q);
-    launch_materials_multi(S, P, Q, g, med, tr, tex, st);
+    if (med) launch_materials_multi_medium(S, P, Q, g, tr, tex, st);
+    else launch_materials_multi(S, P, Q, g, tr, tex, st);
     if (!med) k_shadow<false, true><<<g, 256, 0, st>>>(S, P, Q);
   } else {
     k_shade_logic<false><<<g, 256, 0, st>>>(S, P, Q);
-    launch_materials_single(S, P, Q, g, med, tr, tex, P.c_rec != nullptr && !med, st);
+    if (med) launch_materials_medium(S, P, Q, g, tr, tex, st);  // the cache is refused for scenes with media
+    else if (P.c_rec != nullptr) launch_materials_cache(S, P, Q, g, tr, tex, st);
+    else launch_materials_plain(S, P, Q, g, tr, tex, st);
     if (!med) k_shadow<false, false><<<g, 256, 0, st>>>(S, P, Q);
   }
 }

@@ -357,7 +357,7 @@ struct Shader {
           float pdf = 0.0f;
           float3 f = f3(0.0f);
           if (is_surface) {
-            f = bsdf_eval<MAT>(st.fr, mat, ans, -raydir, st.ffnormal, ldir, pdf);
+            f = bsdf_eval<MAT, false>(st.fr, mat, ans, -raydir, st.ffnormal, ldir, pdf);
           } else {
             pdf = phase_hg(dot(-raydir, ldir), aniso);
             f = f3(pdf);
@@ -386,7 +386,7 @@ struct Shader {
           float pdf = 0.0f;
           float3 f = f3(0.0f);
           if (is_surface) {
-            f = bsdf_eval<MAT>(st.fr, mat, ans, -raydir, st.ffnormal, ls.direction, pdf);
+            f = bsdf_eval<MAT, false>(st.fr, mat, ans, -raydir, st.ffnormal, ls.direction, pdf);
           } else {
             pdf = phase_hg(dot(-raydir, ls.direction), aniso);
             f = f3(pdf);
@@ -581,7 +581,7 @@ __global__ void __launch_bounds__(256, MEDIUM ? 4 : 3) k_shade(const __grid_cons
               pend |= PEND_ENV;
               d0 = make_float4(ldir.x, ldir.y, ldir.z, WORLD_SIZE);
               float pdf;
-              float3 f = bsdf_eval<MAT>(st.fr, mat, ans, -d, st.ffnormal, ldir, pdf);
+              float3 f = bsdf_eval<MAT, !MEDIUM>(st.fr, mat, ans, -d, st.ffnormal, ldir, pdf);
               if (pdf > 0.0f) {
                 float w = power_heuristic(light_pdf, pdf);
                 if (w > 0.0f) c0 = w * em * f / light_pdf;
@@ -598,7 +598,7 @@ __global__ void __launch_bounds__(256, MEDIUM ? 4 : 3) k_shade(const __grid_cons
               pend |= PEND_LIGHT;
               d1 = make_float4(ls.direction.x, ls.direction.y, ls.direction.z, ls.dist - 2.0f * EPS);
               float pdf;
-              float3 f = bsdf_eval<MAT>(st.fr, mat, ans, -d, st.ffnormal, ls.direction, pdf);
+              float3 f = bsdf_eval<MAT, !MEDIUM>(st.fr, mat, ans, -d, st.ffnormal, ls.direction, pdf);
               if (pdf > 0.0f) {
                 float w = 1.0f;
                 if (L.area > 0.0f) w = power_heuristic(ls.pdf, pdf);
@@ -624,7 +624,7 @@ __global__ void __launch_bounds__(256, MEDIUM ? 4 : 3) k_shade(const __grid_cons
         float3 L;
         float pdf;
         uint32_t sflags = 0;
-        float3 f = bsdf_sample<MAT>(sh.rng, ans, st.fr, mat, -d, st.ffnormal, L, pdf, sflags);
+        float3 f = bsdf_sample<MAT, !MEDIUM>(sh.rng, ans, st.fr, mat, -d, st.ffnormal, L, pdf, sflags);
         d = L;
         state_pdf = pdf;
         flags |= sflags & 0xFFu;
@@ -689,6 +689,29 @@ __global__ void __launch_bounds__(256, MEDIUM ? 4 : 3) k_shade(const __grid_cons
     nshadow_total += sh.nshadow;
   }
   if (MEDIUM) count_add(&Q.rays[1], (uint32_t)nshadow_total);
+}
+
+// The three material kernels of one bounce (diffuse, opaque Disney, Disney
+// with a glass lobe) in one feature permutation. Each pt_shade_*.cu
+// instantiates the permutations of one (medium, shared-wavefront, cache)
+// combination, so the variants compile in parallel.
+template <bool MED, bool TR, bool MULTI, bool CACHE, bool TEX>
+inline void launch_three(const DevScene& S, const PathState& P, const QueueSet& Q, int g, cudaStream_t st) {
+  k_shade<PT_MATERIAL_DIFFUSE, MED, TR, MULTI, CACHE, TEX><<<g, 256, 0, st>>>(S, P, Q);
+  k_shade<PT_MATERIAL_DISNEY, MED, TR, MULTI, CACHE, TEX><<<g, 256, 0, st>>>(S, P, Q);
+  k_shade<SHADE_DISNEY_GLASS, MED, TR, MULTI, CACHE, TEX><<<g, 256, 0, st>>>(S, P, Q);
+}
+
+template <bool MED, bool MULTI, bool CACHE>
+inline void launch_permutation(const DevScene& S, const PathState& P, const QueueSet& Q, int g, bool tr, bool tex,
+                               cudaStream_t st) {
+  if (tr) {
+    if (tex) launch_three<MED, true, MULTI, CACHE, true>(S, P, Q, g, st);
+    else launch_three<MED, true, MULTI, CACHE, false>(S, P, Q, g, st);
+  } else {
+    if (tex) launch_three<MED, false, MULTI, CACHE, true>(S, P, Q, g, st);
+    else launch_three<MED, false, MULTI, CACHE, false>(S, P, Q, g, st);
+  }
 }
 
 }  // namespace hpt
