@@ -28,6 +28,8 @@ namespace {
 constexpr int NB = 16;
 constexpr int BUILD_THREADS = 256;
 constexpr int SAH_LEAF_MAX = 4;
+// SAH cost of visiting a node, in units of one triangle test.
+constexpr float SAH_NODE_COST = 0.5f;
 
 struct BuildNode {
   float lo[3];
@@ -262,7 +264,7 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_level(const BuildTask* tasks,
       float area = box_area(box[0], box[1], box[2], box[6], box[7], box[8]);
       if (bi < 0) {
         best_s = (t.count <= (uint32_t)LEAF_MAX) ? -2 : -1;  // -2 leaf, -1 median split
-      } else if (t.count <= (uint32_t)SAH_LEAF_MAX && area * t.count <= bc + 0.5f * area) {
+      } else if (t.count <= (uint32_t)SAH_LEAF_MAX && area * t.count <= bc + SAH_NODE_COST * area) {
         best_s = -2;
       } else {
         best_s = bi;
@@ -533,7 +535,7 @@ __global__ void __launch_bounds__(SUB_WARPS * 32) k_subtree(const BuildTask* tas
       }
       const float area = box_area(v[0], v[1], v[2], v[6], v[7], v[8]);
       if (bi < 0) best = (t.count <= (uint32_t)LEAF_MAX) ? -2 : -1;  // -2 leaf, -1 median split
-      else if (t.count <= (uint32_t)SAH_LEAF_MAX && area * t.count <= bc + 0.5f * area) best = -2;
+      else if (t.count <= (uint32_t)SAH_LEAF_MAX && area * t.count <= bc + SAH_NODE_COST * area) best = -2;
       else best = bi;
       leaf = best == -2;
     }
