@@ -290,14 +290,17 @@ void normal_matrix(const float* T, float N[9]) {
 
 // Shading kernel of a material (MAT_CLASS_*). The glass lobe's weight is
 // (1 - metallic) * specular_transmission, computed as the lobe probabilities
-// compute it; a metallic-roughness map replaces metallic per hit, so there
-// only a zero transmission rules the lobe out.
+// compute it. A weight that is zero or NaN gives a zero or NaN probability,
+// so the lobe is never evaluated or sampled (a negative weight can still
+// give a positive probability through a negative normalisation, so only
+// zero and NaN count). A metallic-roughness map replaces metallic per hit,
+// so there only a zero transmission rules the lobe out.
 uint32_t material_class(const pt_material& m, uint32_t num_textures) {
   if (m.type != PT_MATERIAL_DISNEY) return MAT_CLASS_DIFFUSE;
   if (m.specular_transmission == 0.0f) return MAT_CLASS_DISNEY;
   if (m.metallic_roughness_map_index < num_textures) return MAT_CLASS_GLASS;
   const float glass_wt = (1.0f - m.metallic) * m.specular_transmission;
-  return glass_wt > 0.0f ? MAT_CLASS_GLASS : MAT_CLASS_DISNEY;
+  return (glass_wt > 0.0f || glass_wt < 0.0f) ? MAT_CLASS_GLASS : MAT_CLASS_DISNEY;
 }
 
 void fill_view(pt_renderer* r) {

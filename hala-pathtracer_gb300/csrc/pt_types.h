@@ -153,8 +153,9 @@ constexpr uint32_t IN_MEDIUM_BIT = 0x200u;  // is_in_medium
 
 // Shading kernel of a material (DevScene::mat_class; 0 = the surface-logic
 // kernel: misses, lights, invalid materials). A Disney material whose glass
-// lobe has zero weight, (1 - metallic) * specular_transmission as the lobe
-// probabilities compute it, is shaded by a kernel built without that lobe.
+// lobe weight, (1 - metallic) * specular_transmission as the lobe
+// probabilities compute it, is zero (or NaN) is shaded by a kernel built
+// without that lobe.
 constexpr uint32_t MAT_CLASS_DIFFUSE = 1, MAT_CLASS_DISNEY = 2, MAT_CLASS_GLASS = 3;
 // Template argument of k_shade for the glass-capable Disney kernel.
 constexpr int SHADE_DISNEY_GLASS = 2;
