@@ -212,6 +212,7 @@ void renderer_drop_scene(pt_renderer* r) {
   renderer_drop_build_inputs(r);
   r->vnorm.release();
   r->vtan.release();
+  r->tri_shade.release();
   r->vuv.release();
   r->tri_sorted.release();
   r->nodes.release();
@@ -238,9 +239,10 @@ uint64_t renderer_estimate_bytes(const pt_scene_desc* d, uint32_t width, uint32_
   const uint64_t V = std::max<uint64_t>(nv, 1), T = std::max<uint64_t>(nt, 1);
   // vertices: raw 44 + normal/tangent/position 48 + uv 8
   // triangles: raw indices 12 + v0/e1/e2 48 + sorted 48 + 4-wide nodes
-  // (capacity 2 per triangle) 256 + vertex ids 12 + material 4; the BVH
-  // build's scratch (binary nodes and queues) is about 190 B more
-  uint64_t b = V * 100 + T * (380 + 190);
+  // (capacity 2 per triangle) 256 + vertex ids 12 + material 4 + shading
+  // record 96; the BVH build's scratch (binary nodes and queues) is about
+  // 190 B more
+  uint64_t b = V * 100 + T * (476 + 190);
   b += (uint64_t)d->num_materials * sizeof(pt_material) + 4096;
   for (uint32_t i = 0; i < d->num_textures; ++i) b += 16ull * d->textures[i].width * d->textures[i].height + 16;
   const uint64_t E = (uint64_t)env_w * env_h;
@@ -312,6 +314,7 @@ void fill_view(pt_renderer* r) {
   S.tri_mat = r->tri_mat.p;
   S.vnorm = r->vnorm.p;
   S.vtan = r->vtan.p;
+  S.tri_shade = r->tri_shade.p;
   S.vuv = r->vuv.p;
   S.mats = r->dmats.p;
   S.mat_class = r->dmat_class.p;
@@ -615,6 +618,7 @@ pt_status pt_renderer_set_scene(pt_renderer* r, const pt_scene_desc* s) {
   size_t V = std::max<uint64_t>(nv, 1), T = std::max<uint64_t>(nt, 1);
   CK(r, r->vnorm.ensure(V));
   CK(r, r->vtan.ensure(V));
+  CK(r, r->tri_shade.ensure(6 * T));
   CK(r, r->vuv.ensure(V));
   CK(r, r->wpos.ensure(V));
   CK(r, r->tri_v0.ensure(T));
@@ -654,7 +658,7 @@ pt_status pt_renderer_set_scene(pt_renderer* r, const pt_scene_desc* s) {
   }
   launch_flatten(r->raw_verts.p, r->raw_idx.p, r->dprims.p, (uint32_t)prims.size(), r->nverts, r->ntris, nullptr,
                  nullptr, r->vnorm.p, r->vtan.p, r->vuv.p, r->wpos.p, r->tri_v0.p, r->tri_e1.p, r->tri_e2.p,
-                 r->tri_vidx.p, r->tri_mat.p, st);
+                 r->tri_vidx.p, r->tri_mat.p, r->tri_shade.p, st);
   CK(r, cudaGetLastError());
   CK(r, cudaStreamSynchronize(st));
   r->has_scene = true;

@@ -150,7 +150,7 @@ struct pt_renderer {
   hpt::Buf<float> raw_verts;
   hpt::Buf<uint32_t> raw_idx;
   hpt::Buf<hpt::PrimUpload> dprims;
-  hpt::Buf<float4> vnorm, vtan, wpos, tri_v0, tri_e1, tri_e2, tri_sorted, nodes;
+  hpt::Buf<float4> vnorm, vtan, tri_shade, wpos, tri_v0, tri_e1, tri_e2, tri_sorted, nodes;
   hpt::Buf<float2> vuv;
   hpt::Buf<uint32_t> tri_vidx, tri_mat;
   hpt::Buf<pt_material> dmats;

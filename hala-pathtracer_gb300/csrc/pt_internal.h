@@ -68,7 +68,7 @@ struct PrimUpload {
 void launch_flatten(const float* raw_verts, const uint32_t* raw_idx, const PrimUpload* prims, uint32_t nprims,
                     uint32_t total_verts, uint32_t total_tris, const uint32_t* vert_prim, const uint32_t* tri_prim,
                     float4* vnorm, float4* vtan, float2* vuv, float4* wpos, float4* tri_v0, float4* tri_e1,
-                    float4* tri_e2, uint32_t* tri_vidx, uint32_t* tri_mat, cudaStream_t st);
+                    float4* tri_e2, uint32_t* tri_vidx, uint32_t* tri_mat, float4* tri_shade, cudaStream_t st);
 // FP64 alias tables of the environment map; returns the FP64 luminance sum
 // through *total_out (device pointer to one double).
 // RGB float triples -> RGBA (alpha 0) environment texels.

@@ -48,8 +48,8 @@ __global__ void k_flatten_verts(const float* raw, const PrimUpload* prims, uint3
 }
 
 __global__ void k_flatten_tris(const uint32_t* raw_idx, const PrimUpload* prims, uint32_t nprims, uint32_t ntris,
-                               const float4* wpos, float4* tv0, float4* te1, float4* te2, uint32_t* tvidx,
-                               uint32_t* tmat) {
+                               const float4* wpos, const float4* vnorm, const float4* vtan, float4* tv0, float4* te1,
+                               float4* te2, uint32_t* tvidx, uint32_t* tmat, float4* tshade) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntris) return;
   const PrimUpload& P = prims[find_prim(prims, nprims, t, true)];
@@ -63,6 +63,14 @@ __global__ void k_flatten_tris(const uint32_t* raw_idx, const PrimUpload* prims,
   tvidx[3 * (size_t)t + 1] = b;
   tvidx[3 * (size_t)t + 2] = c;
   tmat[t] = P.material;
+  float4* r = tshade + 6 * (size_t)t;
+  const float4 n0 = vnorm[a];
+  r[0] = make_float4(n0.x, n0.y, n0.z, __uint_as_float(P.material));
+  r[1] = vnorm[b];
+  r[2] = vnorm[c];
+  r[3] = vtan[a];
+  r[4] = vtan[b];
+  r[5] = vtan[c];
 }
 
 // BT.709 luminance in FP64, rounded like the oracle (no contraction).
@@ -213,13 +221,13 @@ __global__ void __launch_bounds__(32) k_env_marginal_warp(const double* row_sums
 void launch_flatten(const float* raw_verts, const uint32_t* raw_idx, const PrimUpload* prims, uint32_t nprims,
                     uint32_t total_verts, uint32_t total_tris, const uint32_t*, const uint32_t*, float4* vnorm,
                     float4* vtan, float2* vuv, float4* wpos, float4* tri_v0, float4* tri_e1, float4* tri_e2,
-                    uint32_t* tri_vidx, uint32_t* tri_mat, cudaStream_t st) {
+                    uint32_t* tri_vidx, uint32_t* tri_mat, float4* tri_shade, cudaStream_t st) {
   if (total_verts)
     k_flatten_verts<<<(total_verts + 255) / 256, 256, 0, st>>>(raw_verts, prims, nprims, total_verts, vnorm, vtan,
                                                                 vuv, wpos);
   if (total_tris)
-    k_flatten_tris<<<(total_tris + 255) / 256, 256, 0, st>>>(raw_idx, prims, nprims, total_tris, wpos, tri_v0,
-                                                              tri_e1, tri_e2, tri_vidx, tri_mat);
+    k_flatten_tris<<<(total_tris + 255) / 256, 256, 0, st>>>(raw_idx, prims, nprims, total_tris, wpos, vnorm, vtan,
+                                                              tri_v0, tri_e1, tri_e2, tri_vidx, tri_mat, tri_shade);
 }
 
 __global__ void k_env_widen(const float* __restrict__ rgb, float4* __restrict__ env, size_t n) {

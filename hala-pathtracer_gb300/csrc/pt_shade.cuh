@@ -210,9 +210,9 @@ struct SurfState {  // the State fields filled by triangles.rchit.glsl:13-76
   uint32_t mat;
 };
 __device__ __forceinline__ float3 interp_normal(const DevScene& S, uint32_t id, float u, float v) {
-  uint32_t i0 = __ldg(&S.tri_vidx[3 * id]), i1 = __ldg(&S.tri_vidx[3 * id + 1]), i2 = __ldg(&S.tri_vidx[3 * id + 2]);
+  const float4* r = S.tri_shade + 6 * (size_t)id;
   float b0 = 1.0f - u - v, b1 = u, b2 = v;
-  float3 n = f3(__ldg(&S.vnorm[i0])) * b0 + f3(__ldg(&S.vnorm[i1])) * b1 + f3(__ldg(&S.vnorm[i2])) * b2;
+  float3 n = f3(__ldg(r)) * b0 + f3(__ldg(r + 1)) * b1 + f3(__ldg(r + 2)) * b2;
   return normalize(n);
 }
 // Texture coordinate of a triangle hit (triangles.rchit.glsl:63).
@@ -226,11 +226,13 @@ __device__ __forceinline__ float2 hit_uv(const DevScene& S, float4 hit) {
 
 __device__ __forceinline__ void fill_surface(const DevScene& S, float3 o, float3 d, float4 hit, SurfState& s) {
   uint32_t id = __float_as_uint(hit.w);
-  uint32_t i0 = __ldg(&S.tri_vidx[3 * id]), i1 = __ldg(&S.tri_vidx[3 * id + 1]), i2 = __ldg(&S.tri_vidx[3 * id + 2]);
+  const float4* r = S.tri_shade + 6 * (size_t)id;
+  const float4 n0 = __ldg(r), n1 = __ldg(r + 1), n2 = __ldg(r + 2);
+  const float4 t0 = __ldg(r + 3), t1 = __ldg(r + 4), t2 = __ldg(r + 5);
   float b0 = 1.0f - hit.y - hit.z, b1 = hit.y, b2 = hit.z;
-  float3 n = f3(__ldg(&S.vnorm[i0])) * b0 + f3(__ldg(&S.vnorm[i1])) * b1 + f3(__ldg(&S.vnorm[i2])) * b2;
+  float3 n = f3(n0) * b0 + f3(n1) * b1 + f3(n2) * b2;
   n = normalize(n);
-  float3 tg = f3(__ldg(&S.vtan[i0])) * b0 + f3(__ldg(&S.vtan[i1])) * b1 + f3(__ldg(&S.vtan[i2])) * b2;
+  float3 tg = f3(t0) * b0 + f3(t1) * b1 + f3(t2) * b2;
   tg = normalize(tg);
   s.hit_distance = hit.x;
   s.fhp = o + d * s.hit_distance;
@@ -238,7 +240,7 @@ __device__ __forceinline__ void fill_surface(const DevScene& S, float3 o, float3
   s.ffnormal = dot(n, d) <= 0.0f ? n : -n;
   s.fr.tangent = tg;
   s.fr.bitangent = cross(n, tg);
-  s.mat = __ldg(&S.tri_mat[id]);
+  s.mat = __float_as_uint(n0.w);
 }
 
 // ------------------------------------------------------------------ material textures

@@ -7,6 +7,10 @@
 //            tri_vidx[3*id]     global vertex indices of triangle id
 //            tri_mat[id]        material index of triangle id
 //            vnorm/vtan[v]      float4 world-space (un-normalised) attributes
+//            tri_shade[6*id]    float4 x6: the normals then the tangents of
+//                               triangle id's three vertices (copies of
+//                               vnorm/vtan; .w of the first = material index
+//                               bits), one dependent fetch for shading -- 96 B
 //            vuv[v]             float2
 //            mats[]             pt_material (the std140 Material field set)
 //            env_rgba[]         float4 per environment texel
@@ -71,6 +75,7 @@ struct DevScene {
   const uint32_t* tri_mat;
   const float4* vnorm;
   const float4* vtan;
+  const float4* tri_shade;
   const float2* vuv;
   const pt_material* mats;
   // per material, which shading kernel takes its hits: MAT_CLASS_*
