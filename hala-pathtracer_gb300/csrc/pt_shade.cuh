@@ -202,6 +202,9 @@ __device__ __forceinline__ LightSample sample_light(uint4& rng, float3 fhp, cons
   return o;
 }
 
+// Any component non-zero (NaN counts as non-zero).
+__device__ __forceinline__ bool nonzero(float3 c) { return c.x != 0.0f || c.y != 0.0f || c.z != 0.0f; }
+
 // ------------------------------------------------------------------ hit -> state
 struct SurfState {  // the State fields filled by triangles.rchit.glsl:13-76
   float3 fhp, ffnormal, normal;
@@ -575,18 +578,24 @@ __global__ void __launch_bounds__(256, MEDIUM ? 4 : 3) k_shade(const __grid_cons
           float3 scatter_pos = fhp + st.ffnormal * EPS;
           float3 c0 = f3(0.0f), c1 = f3(0.0f);
           float4 d0 = make_float4(0, 0, 0, 0), d1 = make_float4(0, 0, 0, 0);
+          // A shadow ray is traced only when its contribution is not zero:
+          // adding a zero (visible or not) leaves the sum unchanged, so only
+          // the visibility events of the hit-sequence hash depend on it (the
+          // oracle hashes the same rays).
           if (S.env_map) {
             float3 em;
             float light_pdf;
             float3 ldir = sample_env_map(S, sh.rng, em, light_pdf);
             if (light_pdf > 0.0f) {
-              pend |= PEND_ENV;
-              d0 = make_float4(ldir.x, ldir.y, ldir.z, WORLD_SIZE);
               float pdf;
               float3 f = bsdf_eval<MAT, !MEDIUM>(st.fr, mat, ans, -d, st.ffnormal, ldir, pdf);
               if (pdf > 0.0f) {
                 float w = power_heuristic(light_pdf, pdf);
                 if (w > 0.0f) c0 = w * em * f / light_pdf;
+              }
+              if (nonzero(c0)) {
+                pend |= PEND_ENV;
+                d0 = make_float4(ldir.x, ldir.y, ldir.z, WORLD_SIZE);
               }
             }
           }
@@ -597,8 +606,6 @@ __global__ void __launch_bounds__(256, MEDIUM ? 4 : 3) k_shade(const __grid_cons
             if (li >= 0 && li < (int)nl) L = S.lights[li];
             LightSample ls = sample_light(sh.rng, fhp, L, nl);
             if (ls.pdf > 0.0f && dot(ls.direction, ls.normal) < 0.0f) {
-              pend |= PEND_LIGHT;
-              d1 = make_float4(ls.direction.x, ls.direction.y, ls.direction.z, ls.dist - 2.0f * EPS);
               float pdf;
               float3 f = bsdf_eval<MAT, !MEDIUM>(st.fr, mat, ans, -d, st.ffnormal, ls.direction, pdf);
               if (pdf > 0.0f) {
@@ -606,8 +613,13 @@ __global__ void __launch_bounds__(256, MEDIUM ? 4 : 3) k_shade(const __grid_cons
                 if (L.area > 0.0f) w = power_heuristic(ls.pdf, pdf);
                 if (w > 0.0f) c1 = w * ls.emission * f / ls.pdf;
               }
+              if (nonzero(c1)) {
+                pend |= PEND_LIGHT;
+                d1 = make_float4(ls.direction.x, ls.direction.y, ls.direction.z, ls.dist - 2.0f * EPS);
+              }
             }
           }
+          if (!pend) rad += T * f3(0.0f);  // radiance += throughput * Ld with Ld = 0 (NaN for a non-finite T)
           if (pend) {
             P.sh_o[p] = make_float4(scatter_pos.x, scatter_pos.y, scatter_pos.z, 0.0f);
             P.sh_d0[p] = d0;

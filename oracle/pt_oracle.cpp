@@ -112,6 +112,8 @@ inline void rand4blue(RNG& r, float out[4]) {
 // ---------------------------------------------------------------- small math
 // common/common.glsl:26-71, common/sampling.glsl
 inline float luminance(V3 c) { return 0.212671f * c.x + 0.715160f * c.y + 0.072169f * c.z; }
+// Any component non-zero (NaN counts as non-zero).
+inline bool nonzero(V3 c) { return c.x != 0.0f || c.y != 0.0f || c.z != 0.0f; }
 inline V3 to_world(V3 X, V3 Y, V3 Z, V3 v) { return v.x * X + v.y * Y + v.z * Z; }
 inline V3 to_local(V3 X, V3 Y, V3 Z, V3 v) { return V3(dot(v, X), dot(v, Y), dot(v, Z)); }
 inline float sin2_theta(V3 w) { return std::fmax(0.0f, 1.0f - w.z * w.z); }
@@ -1420,15 +1422,21 @@ struct Tracer {
             }
           }
         } else {
-          bool occ = occluded(sr, WORLD_SIZE);
-          hmix(hash, 0x40000000u | (occ ? 0u : 1u));
-          if (!occ) {
-            float pdf;
-            V3 f = bsdf_eval(st, mat, ans, -ray.d, st.ffnormal, light_dir, pdf);
-            if (pdf > 0.0f) {
-              float w = power_heuristic(light_pdf, pdf);
-              if (w > 0.0f) Ld += w * Li * f / light_pdf;
-            }
+          // The reference traces the shadow ray and adds the contribution
+          // when it is visible; a zero contribution leaves Ld unchanged
+          // either way, so it is not traced and not hashed (the GPU path
+          // does the same).
+          float pdf;
+          V3 f = bsdf_eval(st, mat, ans, -ray.d, st.ffnormal, light_dir, pdf);
+          V3 contrib(0.0f);
+          if (pdf > 0.0f) {
+            float w = power_heuristic(light_pdf, pdf);
+            if (w > 0.0f) contrib = w * Li * f / light_pdf;
+          }
+          if (nonzero(contrib)) {
+            bool occ = occluded(sr, WORLD_SIZE);
+            hmix(hash, 0x40000000u | (occ ? 0u : 1u));
+            if (!occ) Ld += contrib;
           }
         }
       }
@@ -1465,16 +1473,18 @@ struct Tracer {
             }
           }
         } else {
-          bool occ = occluded(sr, ls.dist - 2.0f * EPS);
-          hmix(hash, 0x50000000u | (occ ? 0u : 1u));
-          if (!occ) {
-            float pdf;
-            V3 f = bsdf_eval(st, mat, ans, -ray.d, st.ffnormal, ls.direction, pdf);
-            if (pdf > 0.0f) {
-              float w = 1.0f;
-              if (L.area > 0.0f) w = power_heuristic(light_pdf, pdf);
-              if (w > 0.0f) Ld += w * Li * f / light_pdf;
-            }
+          float pdf;
+          V3 f = bsdf_eval(st, mat, ans, -ray.d, st.ffnormal, ls.direction, pdf);
+          V3 contrib(0.0f);
+          if (pdf > 0.0f) {
+            float w = 1.0f;
+            if (L.area > 0.0f) w = power_heuristic(light_pdf, pdf);
+            if (w > 0.0f) contrib = w * Li * f / light_pdf;
+          }
+          if (nonzero(contrib)) {
+            bool occ = occluded(sr, ls.dist - 2.0f * EPS);
+            hmix(hash, 0x50000000u | (occ ? 0u : 1u));
+            if (!occ) Ld += contrib;
           }
         }
       }
