@@ -354,7 +354,7 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_level(const BuildTask* tasks,
 // large as the current one, so the stack holds at most log2(SUBTREE_MAX)
 // entries, and a subtree of c triangles has fewer than 2c nodes, which
 // bounds the loop.
-constexpr uint32_t SUBTREE_MAX = 256;
+constexpr uint32_t SUBTREE_MAX = 128;
 constexpr int SUB_WARPS = 8;
 constexpr int SUB_STACK = 16;
 
