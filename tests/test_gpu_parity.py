@@ -253,3 +253,21 @@ def test_every_disney_kernel_matches_the_oracle(pt, scenes, oracle_mod):
     rad_o, hash_o = o.trace_paths(np.arange(WH), 0, sc.spp)
     assert np.array_equal(hash_g, hash_o.reshape(-1))
     assert np.array_equal(rad_g.view(np.uint32), rad_o.reshape(-1, 3).view(np.uint32))
+
+
+@pytest.mark.parametrize("size", [(16384, 4), (2048, 1024)])
+def test_env_alias_tables_both_builders(pt, scenes, oracle_mod, size):
+    """The environment's alias tables come from the one-warp-per-row builder
+    when a row fits in shared memory (2048 wide) and from the one-thread-per-
+    row builder otherwise (16384 texels x 16 B per row): per-path radiance
+    and hit sequences equal the oracle's bit for bit either way."""
+    sc = scenes.tiny_variants()["disney"]
+    sc.env_rgb = scenes.synthetic_sky(*size)
+    r = pt.renderer_for(sc, keep_samples=True)
+    r.render(sc.spp)
+    rad_g, hash_g = r.samples()
+    o = oracle_mod.Oracle(sc)
+    WH = sc.width * sc.height
+    rad_o, hash_o = o.trace_paths(np.arange(WH), 0, sc.spp)
+    assert np.array_equal(hash_g, hash_o.reshape(-1))
+    assert np.array_equal(rad_g.view(np.uint32), rad_o.reshape(-1, 3).view(np.uint32))
