@@ -620,12 +620,16 @@ __global__ void __launch_bounds__(256, MEDIUM ? 4 : 3) k_shade(const __grid_cons
             }
           }
           if (!pend) rad += T * f3(0.0f);  // radiance += throughput * Ld with Ld = 0 (NaN for a non-finite T)
-          if (pend) {
+          if (pend) {  // k_shadow reads only the records of the pending rays
             P.sh_o[p] = make_float4(scatter_pos.x, scatter_pos.y, scatter_pos.z, 0.0f);
-            P.sh_d0[p] = d0;
-            P.sh_d1[p] = d1;
-            P.sh_c0[p] = make_float4(c0.x, c0.y, c0.z, 0.0f);
-            P.sh_c1[p] = make_float4(c1.x, c1.y, c1.z, 0.0f);
+            if (pend & PEND_ENV) {
+              P.sh_d0[p] = d0;
+              P.sh_c0[p] = make_float4(c0.x, c0.y, c0.z, 0.0f);
+            }
+            if (pend & PEND_LIGHT) {
+              P.sh_d1[p] = d1;
+              P.sh_c1[p] = make_float4(c1.x, c1.y, c1.z, 0.0f);
+            }
             P.sh_T[p] = make_float4(T.x, T.y, T.z, 0.0f);
           }
         }
