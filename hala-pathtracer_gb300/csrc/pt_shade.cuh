@@ -686,16 +686,18 @@ __global__ void __launch_bounds__(256, MEDIUM ? 4 : 3) k_shade(const __grid_cons
       if (pend & PEND_STOP) hmix(sh.hash, 0x61000000u);
       if (pend & PEND_RR) hmix(sh.hash, 0x72000000u);
     }
-    P.rng[p] = sh.rng;
-    P.ray_o[p] = make_float4(o.x, o.y, o.z, 0.0f);
-    P.ray_d[p] = make_float4(d.x, d.y, d.z, 0.0f);
-    P.thr[p] = make_float4(T.x, T.y, T.z, state_pdf);
     P.rad[p] = make_float4(rad.x, rad.y, rad.z, __uint_as_float(sh.hash));
-    P.depth[p] = depth + 1;  // loop increment of pathtracer.rgen.glsl:55
-    P.flags[p] = (flags & ~(ANS_BIT | IN_MEDIUM_BIT)) | (ans ? ANS_BIT : 0u) | (in_medium ? IN_MEDIUM_BIT : 0u);
-    if (MEDIUM) {
-      P.med0[p] = m0;
-      P.med1[p] = m1;
+    if (!stop) {  // a path that ends here is only read again for its radiance
+      P.rng[p] = sh.rng;
+      P.ray_o[p] = make_float4(o.x, o.y, o.z, 0.0f);
+      P.ray_d[p] = make_float4(d.x, d.y, d.z, 0.0f);
+      P.thr[p] = make_float4(T.x, T.y, T.z, state_pdf);
+      P.depth[p] = depth + 1;  // loop increment of pathtracer.rgen.glsl:55
+      P.flags[p] = (flags & ~(ANS_BIT | IN_MEDIUM_BIT)) | (ans ? ANS_BIT : 0u) | (in_medium ? IN_MEDIUM_BIT : 0u);
+      if (MEDIUM) {
+        P.med0[p] = m0;
+        P.med1[p] = m1;
+      }
     }
     if (deferred) {
       float4 so = P.sh_o[p];
