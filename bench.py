@@ -8,10 +8,13 @@ is the 9x9 Disney sphere grid under a 2048x1024 HDR sky, 1920x1080, 64 spp,
 depth 12, Russian roulette from depth 4, all synthetic.
 
 `value` is paths/s with the scene already resident in HBM (device time of the
-K timed renders, CUDA events on the renderer's stream). `e2e` is the same
+K timed renders, CUDA events on the renderer's stream; each wave's bounces
+run as one CUDA graph launch unless --bounce-loop host). `e2e` is the same
 metric through the public API from host buffers: scene upload, BVH build,
 environment tables, the render and the image read-back are all inside its
-timed region.
+timed region. The roofline's closest-hit launch times come from K further
+renders of the same workload with CUDA events around every launch (the
+host-driven bounce loop; events cannot sit inside the graph).
 
 --impl reference times the CPU restatement of the reference integrator on
 the host cores over a bounded sample of the same workload.
