@@ -822,7 +822,7 @@ pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) {
   r->stats.closest_rays = r->stats.shadow_rays = 0;
   r->stats.render_ms = 0.0;
   if (total == 0) return PT_OK;
-  uint64_t want = r->cfg.wave_paths ? r->cfg.wave_paths : (1u << 25);
+  uint64_t want = r->cfg.wave_paths ? r->cfg.wave_paths : (1u << 27);  // 2^27 paths: about 35 GB of path state
   if (r->cache_on) want = std::min<uint64_t>(want, r->cache_cfg.paths_per_pass);
   uint32_t cap = (uint32_t)std::min<uint64_t>(want, total);
   const bool med = (r->features & PT_FEATURE_MEDIUM) != 0;

@@ -177,7 +177,7 @@ typedef struct pt_tracer_config {
   int32_t use_simple_aces;
   uint32_t seed;
   uint64_t max_samples;   /* 0 = unlimited */
-  uint32_t wave_paths;    /* paths in flight per wavefront; 0 = library default */
+  uint32_t wave_paths;    /* paths in flight per wavefront; 0 = 1 << 27 (about 35 GB) */
   uint32_t keep_samples;  /* 1 = keep per-path radiance and hit-sequence hash of the last render call */
 } pt_tracer_config;
 
