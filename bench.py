@@ -46,7 +46,7 @@ DEFAULT_WORKLOAD = "disney_grid_1080p_64spp"
 L2_FLUSH_BYTES = 256 << 20  # > 129 MB L2
 # DRAM bytes (read + write) per closest-hit ray of k_trace, from the ncu
 # capture in profiles/k_trace_disney_grid_480x270_bvh4.md (bounces 0 and 1).
-TRACE_DRAM_BYTES_PER_RAY = (349.191168e6 + 173.670912e6 + 287.307520e6 + 114.504448e6) / (8294400 + 5583360)
+TRACE_DRAM_BYTES_PER_RAY = (347.765504e6 + 167.930624e6 + 304.260864e6 + 111.250176e6) / (8294400 + 5583360)
 
 
 def _dist():
