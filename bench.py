@@ -30,6 +30,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -84,7 +85,9 @@ def _peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms into a CSV
+    (in $PT_BENCH_CLOCKS_DIR, else the temporary directory); the JSON line
+    carries the median SM clock under load and the throttle reasons seen."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -92,7 +95,8 @@ class ClockSampler:
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{gpu_index}.csv")
+        out_dir = os.environ.get("PT_BENCH_CLOCKS_DIR", tempfile.gettempdir())
+        self.path = os.path.join(out_dir, f"hala_pt_clocks_rank{gpu_index}.csv")
 
     def start(self):
         try:
