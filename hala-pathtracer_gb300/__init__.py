@@ -161,6 +161,21 @@ class Renderer:
         self._check(self._lib.pt_renderer_read_image(self._h, abi.IMAGE_SAMPLE_HASH, hsh.ctypes.data, hsh.nbytes))
         return rad, hsh
 
+    def read_samples(self, paths):
+        """Per-path radiance (n, 3) and hash (n,) of the last render call for the
+        path indices `paths` (k = frame_local * W * H + pixel), gathered on the
+        device (needs keep_samples)."""
+        idx = np.ascontiguousarray(paths, np.uint64)
+        rad = np.empty((len(idx), 3), np.float32)
+        hsh = np.empty((len(idx),), np.uint32)
+        self._check(self._lib.pt_renderer_read_samples(self._h, idx.ctypes.data, len(idx), rad.ctypes.data,
+                                                       hsh.ctypes.data))
+        return rad, hsh
+
+    def set_traversal_limits(self, stack_entries=0, max_visits=0):
+        """Traversal stack entries (1..96) and node visits per ray; 0 = default."""
+        self._check(self._lib.pt_renderer_set_traversal_limits(self._h, int(stack_entries), int(max_visits)))
+
     def stats(self):
         s = abi.Stats()
         self._check(self._lib.pt_renderer_get_stats(self._h, C.byref(s)))

@@ -15,10 +15,11 @@ PT_ERR_NOT_READY = 5
 PT_ERR_UNSUPPORTED = 6
 PT_ERR_STATE = 7
 PT_ERR_CANCELLED = 8
+PT_ERR_TRAVERSAL = 9
 
 STATUS_NAMES = {
     0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA_ERROR", 4: "TIMEOUT",
-    5: "NOT_READY", 6: "UNSUPPORTED", 7: "BAD_STATE", 8: "CANCELLED",
+    5: "NOT_READY", 6: "UNSUPPORTED", 7: "BAD_STATE", 8: "CANCELLED", 9: "TRAVERSAL_LIMIT",
 }
 
 PT_MAX_CAMERAS = 8
@@ -106,7 +107,8 @@ class Stats(C.Structure):
                 ("trav_nodes", C.c_uint64), ("trav_tris", C.c_uint64),
                 ("kernel_launches", C.c_uint64), ("cache_queries", C.c_uint64),
                 ("cache_train_samples", C.c_uint64), ("cache_train_steps", C.c_uint64),
-                ("cache_loss", C.c_double)]
+                ("cache_loss", C.c_double), ("wave_paths", C.c_uint64),
+                ("bvh_binary_nodes", C.c_uint64)]
 
 
 class CacheConfig(C.Structure):
@@ -199,6 +201,8 @@ RENDERER_SIGNATURES = {
     "pt_renderer_set_profiling": (C.c_int, [C.c_void_p, C.c_uint32]),
     "pt_renderer_trace_rays": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_uint32,
                                          C.c_int32, C.c_int32, C.POINTER(C.c_uint32)]),
+    "pt_renderer_set_traversal_limits": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32]),
+    "pt_renderer_read_samples": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     "pt_bvh_build_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
                                        C.c_uint32, C.c_void_p, C.POINTER(C.c_uint32), C.c_void_p,
                                        C.c_char_p, C.c_size_t]),

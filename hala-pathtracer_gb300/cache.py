@@ -85,3 +85,26 @@ class RadianceCache:
         a, b = C.c_double(), C.c_double()
         self._check(self._lib.pt_cache_benchmark(self._h, int(n), int(iterations), C.byref(a), C.byref(b)))
         return a.value, b.value
+
+
+def main(argv=None):
+    """Device-timed cache kernels on seeded records (profiling entry point):
+    python hala-pathtracer_gb300/cache.py --queries N --iterations K"""
+    import argparse
+    ap = argparse.ArgumentParser(description="radiance-cache kernel benchmark")
+    ap.add_argument("--queries", type=int, default=1 << 22)
+    ap.add_argument("--iterations", type=int, default=5)
+    args = ap.parse_args(argv)
+    c = RadianceCache()
+    infer_ms, train_ms = c.benchmark(args.queries, args.iterations)
+    c.close()
+    print(f"{args.queries} records: inference {infer_ms:.3f} ms, training pass {train_ms:.3f} ms")
+    return 0
+
+
+if __name__ == "__main__":
+    import importlib
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    sys.exit(importlib.import_module("hala-pathtracer_gb300.cache").main())

@@ -95,6 +95,22 @@ cudaError_t WaveBuffers::ensure(uint32_t want, bool want_med, bool want_multi) {
   return cudaSuccess;
 }
 
+void WaveBuffers::release() {
+  graph.reset();
+  Buf<uint4>* b4[] = {&rng};
+  for (auto* b : b4) b->release();
+  Buf<float4>* f4[] = {&ray_o, &ray_d, &hit, &thr, &rad, &albedo, &normal, &med0,
+                       &sh_o, &sh_d0, &sh_d1, &sh_c0, &sh_c1, &sh_T};
+  for (auto* b : f4) b->release();
+  med1.release();
+  Buf<uint32_t>* u[] = {&depth, &flags, &job, &q_a, &q_b, &q_logic, &q_diff, &q_dis, &q_glass, &q_shadow, &counters};
+  for (auto* b : u) b->release();
+  rays.release();
+  cap = 0;
+  med = multi = false;
+  P = PathState{};
+}
+
 uint64_t WaveBuffers::bytes_per_path(bool med, bool multi) {
   // rng 16, ray_o/ray_d/hit/thr/rad/albedo/normal 7x16, depth+flags 8,
   // six NEE float4 96, seven queues 28 (+ medium 24, + job slot 4)
@@ -169,19 +185,24 @@ pt_status validate_scene_desc(const pt_scene_desc* s, std::string* why) {
     if (t.width == 0 || t.height == 0 || !t.rgba) return bad(PT_ERR_INVALID_ARG, "empty texture");
     if ((uint64_t)t.width * t.height > (1ull << 28)) return bad(PT_ERR_UNSUPPORTED, "texture larger than 2^28 texels");
   }
+  // Sizes first: a leaf link holds the first triangle of its leaf in 26 bits,
+  // so a scene of 2^26 triangles or more cannot be traversed.
   uint64_t nv = 0, nt = 0;
   for (uint32_t i = 0; i < s->num_primitives; ++i) {
     const pt_primitive& p = s->primitives[i];
     if (p.num_indices % 3 != 0) return bad(PT_ERR_INVALID_ARG, "index count is not a multiple of 3");
     if ((p.num_vertices && !p.vertices) || (p.num_indices && !p.indices))
       return bad(PT_ERR_INVALID_ARG, "primitive arrays are null");
-    for (uint32_t k = 0; k < p.num_indices; ++k)
-      if (p.indices[k] >= p.num_vertices) return bad(PT_ERR_INVALID_ARG, "index out of range");
     nv += p.num_vertices;
     nt += p.num_indices / 3;
   }
   if (nt >= (1ull << 26) || nv >= (1ull << 31))
     return bad(PT_ERR_UNSUPPORTED, "scene exceeds 2^26 triangles or 2^31 vertices");
+  for (uint32_t i = 0; i < s->num_primitives; ++i) {
+    const pt_primitive& p = s->primitives[i];
+    for (uint32_t k = 0; k < p.num_indices; ++k)
+      if (p.indices[k] >= p.num_vertices) return bad(PT_ERR_INVALID_ARG, "index out of range");
+  }
   return PT_OK;
 }
 
@@ -362,6 +383,39 @@ void fill_view(pt_renderer* r) {
   S.tex_texels = r->tex_texels.p;
   S.tex_info = r->tex_info.p;
   S.num_textures = r->num_textures;
+  S.trav_stack = r->trav_stack;
+  S.trav_visits = r->trav_visits;
+  S.err = r->errw.p;
+}
+
+// Reads and clears the traversal error word (stream-ordered; synchronises).
+pt_status check_traversal(pt_renderer* r) {
+  uint32_t* h = r->pinned + 8;
+  CK(r, cudaMemcpyAsync(h, r->errw.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, r->stream));
+  CK(r, cudaStreamSynchronize(r->stream));
+  const uint32_t w = *h;
+  if (w == 0) return PT_OK;
+  CK(r, cudaMemsetAsync(r->errw.p, 0, sizeof(uint32_t), r->stream));
+  std::string m = "BVH traversal exceeded its limits (";
+  if (w & 1u) m += "stack of " + std::to_string(std::min<uint32_t>(r->trav_stack, 96)) + " entries full";
+  if ((w & 3u) == 3u) m += ", ";
+  if (w & 2u) m += std::to_string(r->trav_visits) + " node visits";
+  m += "); the results of this call may be wrong";
+  return fail(r, PT_ERR_TRAVERSAL, m);
+}
+
+// Default wavefront size: the paths half the free device memory holds, a
+// power of two between 2^16 and 2^27.
+uint32_t default_wave_paths(bool med) {
+  size_t fr = 0, tot = 0;
+  if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+    cudaGetLastError();
+    return 1u << 24;
+  }
+  const uint64_t fit = (uint64_t)(fr / 2) / WaveBuffers::bytes_per_path(med, false);
+  uint32_t w = 1u << 27;
+  while (w > (1u << 16) && w > fit) w >>= 1;
+  return w;
 }
 
 bool write_pfm(const char* path, const float4* px, uint32_t w, uint32_t h) {
@@ -537,10 +591,12 @@ pt_status hpt::renderer_create_with_priority(const pt_tracer_config* cfg, int pr
   }
   size_t WH = (size_t)cfg->width * cfg->height;
   AllocScope as(r->stream);
-  if (r->accum.ensure(WH) || r->albedo.ensure(WH) || r->normal.ensure(WH) || r->final_img.ensure(WH)) {
+  if (r->accum.ensure(WH) || r->albedo.ensure(WH) || r->normal.ensure(WH) || r->final_img.ensure(WH) ||
+      r->errw.ensure(1)) {
     pt_renderer_destroy(r);
     return PT_ERR_OOM;
   }
+  cudaMemsetAsync(r->errw.p, 0, sizeof(uint32_t), r->stream);
   cudaMemsetAsync(r->accum.p, 0, WH * sizeof(float4), r->stream);
   cudaMemsetAsync(r->albedo.p, 0, WH * sizeof(float4), r->stream);
   cudaMemsetAsync(r->normal.p, 0, WH * sizeof(float4), r->stream);
@@ -785,7 +841,9 @@ pt_status pt_renderer_commit(pt_renderer* r) {
     if (rc == 2) return fail(r, PT_ERR_OOM, "BVH collapse: out of device memory");
     if (rc != 0) return fail(r, PT_ERR_CUDA, "BVH collapse failed (code " + std::to_string(rc) + ")");
     r->nnodes = nn4;
+    r->stats.bvh_binary_nodes = nn;
   } else {
+    r->stats.bvh_binary_nodes = 0;
     CK(r, r->nodes.ensure(8));
     r->nnodes = 0;
   }
@@ -822,11 +880,23 @@ pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) {
   r->stats.closest_rays = r->stats.shadow_rays = 0;
   r->stats.render_ms = 0.0;
   if (total == 0) return PT_OK;
-  uint64_t want = r->cfg.wave_paths ? r->cfg.wave_paths : (1u << 27);  // 2^27 paths: about 35 GB of path state
+  const bool med = (r->features & PT_FEATURE_MEDIUM) != 0;
+  const bool auto_wave = r->cfg.wave_paths == 0;
+  uint64_t want = auto_wave ? (r->W.cap ? r->W.cap : default_wave_paths(med)) : r->cfg.wave_paths;
   if (r->cache_on) want = std::min<uint64_t>(want, r->cache_cfg.paths_per_pass);
   uint32_t cap = (uint32_t)std::min<uint64_t>(want, total);
-  const bool med = (r->features & PT_FEATURE_MEDIUM) != 0;
-  CK(r, r->W.ensure(cap, med, false));
+  for (;;) {
+    cudaError_t we = r->W.ensure(cap, med, false);
+    if (we == cudaSuccess) break;
+    // the default size steps down while the device cannot hold it
+    if (we != cudaErrorMemoryAllocation || !auto_wave || cap <= (1u << 16)) {
+      r->W.release();
+      return cuda_fail(r, we, "wavefront buffers");
+    }
+    cudaGetLastError();
+    r->W.release();
+    cap >>= 1;
+  }
   if (!r->cache_on) cap = r->W.cap;  // a larger wavefront already allocated costs nothing more
   cudaStream_t st = r->stream;
   const uint64_t g_start = r->frame_index * WH;
@@ -836,6 +906,7 @@ pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) {
     r->keep_count = total;
   }
   CK(r, cudaMemsetAsync(r->W.rays.p, 0, 4 * sizeof(unsigned long long), st));
+  CK(r, cudaMemsetAsync(r->errw.p, 0, sizeof(uint32_t), st));
   CK(r, cudaEventRecord(r->ev0, st));
   uint32_t max_bounces = 0;
   uint64_t launches = 0;
@@ -915,6 +986,7 @@ pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) {
   r->stats.trav_tris = rays[3];
   r->stats.trace_launches = ntimed;
   r->stats.kernel_launches = launches + 1;  // + finalize
+  r->stats.wave_paths = cap;
   r->stats.cache_queries = c_queries;
   r->stats.cache_train_samples = c_samples;
   r->stats.cache_train_steps = c_steps;
@@ -930,7 +1002,7 @@ pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) {
     tms += e;
   }
   r->stats.trace_ms = tms;
-  return PT_OK;
+  return check_traversal(r);
 }
 
 pt_status pt_renderer_set_radiance_cache(pt_renderer* r, const pt_cache_config* cfg) {
@@ -1101,10 +1173,52 @@ pt_status pt_renderer_trace_rays(pt_renderer* r, const float* rays, uint32_t n, 
   CK(r, dr.ensure(2 * (size_t)n));
   CK(r, dh.ensure(n));
   CK(r, cudaMemcpyAsync(dr.p, rays, 32 * (size_t)n, cudaMemcpyHostToDevice, r->stream));
+  CK(r, cudaMemsetAsync(r->errw.p, 0, sizeof(uint32_t), r->stream));
   launch_trace_rays(r->view, dr.p, n, any_hit, brute, dh.p, r->stream);
   CK(r, cudaGetLastError());
   CK(r, cudaMemcpyAsync(hits, dh.p, 16 * (size_t)n, cudaMemcpyDeviceToHost, r->stream));
   CK(r, cudaStreamSynchronize(r->stream));
+  return check_traversal(r);
+}
+
+pt_status pt_renderer_set_traversal_limits(pt_renderer* r, uint32_t stack_entries, uint32_t max_visits) {
+  if (!r) return PT_ERR_INVALID_ARG;
+  if (stack_entries > 96) return fail(r, PT_ERR_INVALID_ARG, "the traversal stack holds at most 96 entries");
+  r->trav_stack = stack_entries ? stack_entries : 96;
+  r->trav_visits = max_visits ? max_visits : (1u << 22);
+  r->view.trav_stack = r->trav_stack;
+  r->view.trav_visits = r->trav_visits;
+  return PT_OK;
+}
+
+pt_status pt_renderer_read_samples(pt_renderer* r, const uint64_t* paths, uint32_t n, float* radiance,
+                                   uint32_t* hash) {
+  if (!r) return PT_ERR_INVALID_ARG;
+  AllocScope alloc_scope(r->stream);
+  if (!r->cfg.keep_samples) return fail(r, PT_ERR_STATE, "keep_samples is off");
+  if (n == 0) return PT_OK;
+  if (!paths) return fail(r, PT_ERR_INVALID_ARG, "path index array is null");
+  for (uint32_t i = 0; i < n; ++i)
+    if (paths[i] >= r->keep_count) return fail(r, PT_ERR_INVALID_ARG, "path index beyond the last render call");
+  Buf<uint64_t> di;
+  Buf<float4> dr;
+  Buf<uint32_t> dh;
+  CK(r, di.ensure(n));
+  CK(r, dr.ensure(n));
+  CK(r, dh.ensure(n));
+  CK(r, cudaMemcpyAsync(di.p, paths, sizeof(uint64_t) * n, cudaMemcpyHostToDevice, r->stream));
+  launch_gather_samples(r->keep_rad.p, r->keep_hash.p, di.p, n, dr.p, dh.p, r->stream);
+  CK(r, cudaGetLastError());
+  std::vector<float4> tmp(n);
+  CK(r, cudaMemcpyAsync(tmp.data(), dr.p, sizeof(float4) * n, cudaMemcpyDeviceToHost, r->stream));
+  if (hash) CK(r, cudaMemcpyAsync(hash, dh.p, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, r->stream));
+  CK(r, cudaStreamSynchronize(r->stream));
+  if (radiance)
+    for (uint32_t i = 0; i < n; ++i) {
+      radiance[3 * i] = tmp[i].x;
+      radiance[3 * i + 1] = tmp[i].y;
+      radiance[3 * i + 2] = tmp[i].z;
+    }
   return PT_OK;
 }
 

@@ -12,6 +12,7 @@
 // order. A layout pass then writes the 64-byte binary nodes and the
 // triangles in leaf order; k_collapse turns the binary tree into the 4-wide
 // traversal nodes.
+#include <cuda.h>  // driver types only (the driver call is reached through cudaGetDriverEntryPointByVersion)
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -1206,22 +1207,59 @@ constexpr size_t NA_BYTES = align256(NA_OFF_NOD + 2 * NA_MAX * sizeof(BuildNode)
 
 static __device__ __align__(256) unsigned char g_bvh_noalloc_scratch[NA_BYTES];
 
-// Device address of the scratch array, looked up once per device with that
-// device current. In host code the symbol itself is only a host-side stand-in.
+// Device address of the scratch array, looked up with the device current
+// the first time a context uses it. In host code the symbol itself is only a
+// host-side stand-in. The cache is keyed by the context's unique id as well
+// as the device: after cudaDeviceReset the module is loaded again in a new
+// context, possibly at another address, and the lookup is repeated.
 std::mutex g_na_mutex;
 void* g_na_ptr[64] = {};
+unsigned long long g_na_ctx[64] = {};
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+// Unique id of the current context (0 when the driver cannot say).
+unsigned long long current_context_id() {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static bool looked = false;
+  if (!looked) {
+    looked = true;
+    cudaDriverEntryPointQueryResult q1, q2;
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+        q1 == cudaDriverEntryPointSuccess && q2 == cudaDriverEntryPointSuccess) {
+      get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+      get_id = reinterpret_cast<CtxGetIdFn>(f2);
+    } else {
+      cudaGetLastError();
+    }
+  }
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS)
+    return 0;
+  return id;
+}
 
 cudaError_t noalloc_scratch(unsigned char** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  // makes the device's primary context current (initialising it) before its id is read
+  if ((e = cudaSetDevice(dev)) != cudaSuccess) return e;
+  const unsigned long long ctx = current_context_id();
   std::lock_guard<std::mutex> lock(g_na_mutex);
-  if (!g_na_ptr[dev]) {
+  if (!g_na_ptr[dev] || ctx == 0 || g_na_ctx[dev] != ctx) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_bvh_noalloc_scratch);
     if (e != cudaSuccess) return e;
     g_na_ptr[dev] = p;
+    g_na_ctx[dev] = ctx;
   }
   *out = static_cast<unsigned char*>(g_na_ptr[dev]);
   return cudaSuccess;
@@ -1276,11 +1314,14 @@ extern "C" pt_status pt_bvh_build_noalloc(const void* tri_v0, const void* tri_e1
   const float4* e2 = static_cast<const float4*>(tri_e2);
   // The array keeps the previous call's contents: the root task and the
   // counters are rewritten here; every other word is written before it is read.
+  auto cuda_err = [&](cudaError_t x) { return na_fail(error_message, error_capacity, PT_ERR_CUDA, cudaGetErrorString(x)); };
   k_prep<<<(n + 255) / 256, 256, 0, st>>>(v0, e1, e2, n, tlo, thi, tc, ids_a);
+  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e);
+  // pageable sources: the copies have finished reading them when the calls return
   BuildTask root{0, 0, n, 0};
   uint32_t init[4] = {1, 1, 0, 0};
-  cudaMemcpyAsync(tasks_a, &root, sizeof(root), cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(counters, init, sizeof(init), cudaMemcpyHostToDevice, st);
+  if ((e = cudaMemcpyAsync(tasks_a, &root, sizeof(root), cudaMemcpyHostToDevice, st)) != cudaSuccess) return cuda_err(e);
+  if ((e = cudaMemcpyAsync(counters, init, sizeof(init), cudaMemcpyHostToDevice, st)) != cudaSuccess) return cuda_err(e);
   uint32_t ntasks = 1;
   BuildTask* cur = tasks_a;
   BuildTask* nxt = tasks_b;
@@ -1289,15 +1330,17 @@ extern "C" pt_status pt_bvh_build_noalloc(const void* tri_v0, const void* tri_e1
   int cur_slot = 1, nxt_slot = 2;
   uint32_t host_count = 0;
   for (int level = 0; level < 200 && ntasks > 0; ++level) {
-    cudaMemsetAsync(counters + nxt_slot, 0, sizeof(uint32_t), st);
+    if ((e = cudaMemsetAsync(counters + nxt_slot, 0, sizeof(uint32_t), st)) != cudaSuccess) return cuda_err(e);
     ChildLists next;
     next.tasks = nxt;
     next.count = counters + nxt_slot;
     k_level<<<ntasks, BUILD_THREADS, 0, st>>>(cur, counters + cur_slot, src, dst, final_ids, tlo, thi, tc, nodes,
                                               counters, next);
-    cudaMemcpyAsync(&host_count, counters + nxt_slot, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
-    e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) return na_fail(error_message, error_capacity, PT_ERR_CUDA, cudaGetErrorString(e));
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e);
+    if ((e = cudaMemcpyAsync(&host_count, counters + nxt_slot, sizeof(uint32_t), cudaMemcpyDeviceToHost, st)) !=
+        cudaSuccess)
+      return cuda_err(e);
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_err(e);
     ntasks = host_count;
     std::swap(cur, nxt);
     std::swap(src, dst);
@@ -1305,9 +1348,11 @@ extern "C" pt_status pt_bvh_build_noalloc(const void* tri_v0, const void* tri_e1
   }
   if (ntasks != 0) return na_fail(error_message, error_capacity, PT_ERR_CUDA, "BVH build did not terminate");
   uint32_t nn = 0;
-  cudaMemcpyAsync(&nn, counters, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
-  e = cudaStreamSynchronize(st);
-  if (e != cudaSuccess) return na_fail(error_message, error_capacity, PT_ERR_CUDA, cudaGetErrorString(e));
+  if ((e = cudaMemcpyAsync(&nn, counters, sizeof(uint32_t), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+    return cuda_err(e);
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_err(e);
+  if (nn == 0 || nn > node_capacity)
+    return na_fail(error_message, error_capacity, PT_ERR_CUDA, "BVH build produced an invalid node count");
   k_layout<<<(nn + 255) / 256, 256, 0, st>>>(nodes, nn, static_cast<float4*>(nodes_out));
   k_reorder<<<(n + 255) / 256, 256, 0, st>>>(final_ids, n, v0, e1, e2, static_cast<float4*>(tri_sorted_out));
   e = cudaGetLastError();

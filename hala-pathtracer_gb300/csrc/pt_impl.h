@@ -97,6 +97,8 @@ struct WaveBuffers {
   PathState P{};
   BounceGraph graph;
   cudaError_t ensure(uint32_t cap, bool med, bool multi);
+  // Frees every buffer and the bounce graph (cap back to 0).
+  void release();
   // Bytes one path slot occupies (state + queues), for memory budgets.
   static uint64_t bytes_per_path(bool med, bool multi);
 };
@@ -186,6 +188,9 @@ struct pt_renderer {
   pt_stats stats{};
   uint32_t profiling = 0;
   std::vector<cudaEvent_t> tev;  // start/stop pairs around closest-hit launches
+  // traversal limits and the device word their violations set (TRAV_ERR_*)
+  uint32_t trav_stack = 96, trav_visits = 1u << 22;
+  hpt::Buf<uint32_t> errw;
 
   // radiance cache (pt_renderer_set_radiance_cache)
   bool cache_on = false;

@@ -52,6 +52,9 @@ void launch_accumulate(const PathState& P, uint64_t g0, uint32_t n, uint32_t WH,
 void launch_cache_targets(const PathState& P, uint32_t n, float4* tgt, cudaStream_t st);
 void launch_finalize(const float4* accum, uchar4* final_img, uint32_t WH, float ev, int enable, int aces, int simple,
                      cudaStream_t st);
+// out_rad[i] / out_hash[i] = keep_rad / keep_hash at idx[i] (indices checked by the caller).
+void launch_gather_samples(const float4* keep_rad, const uint32_t* keep_hash, const uint64_t* idx, uint32_t n,
+                           float4* out_rad, uint32_t* out_hash, cudaStream_t st);
 void launch_trace_rays(const DevScene& S, const float4* rays, uint32_t n, int any_hit, int brute, uint4* hits,
                        cudaStream_t st);
 

@@ -266,6 +266,15 @@ __global__ void k_trace_rays(const __grid_constant__ DevScene S, const float4* r
   }
 }
 
+__global__ void k_gather_samples(const float4* keep_rad, const uint32_t* keep_hash, const uint64_t* idx, uint32_t n,
+                                 float4* out_rad, uint32_t* out_hash) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint64_t k = idx[i];
+  out_rad[i] = keep_rad[k];
+  out_hash[i] = keep_hash[k];
+}
+
 // ------------------------------------------------------------------ launchers
 // One thread per queued item (the queue length is at most max_items): the
 // block scheduler then balances long and short traversals across SMs.
@@ -330,6 +339,11 @@ void launch_accumulate(const PathState& P, uint64_t g0, uint32_t n, uint32_t WH,
 void launch_finalize(const float4* accum, uchar4* final_img, uint32_t WH, float ev, int enable, int aces, int simple,
                      cudaStream_t st) {
   k_finalize<<<(WH + 255) / 256, 256, 0, st>>>(accum, final_img, WH, ev, enable, aces, simple);
+}
+
+void launch_gather_samples(const float4* keep_rad, const uint32_t* keep_hash, const uint64_t* idx, uint32_t n,
+                           float4* out_rad, uint32_t* out_hash, cudaStream_t st) {
+  k_gather_samples<<<(n + 255) / 256, 256, 0, st>>>(keep_rad, keep_hash, idx, n, out_rad, out_hash);
 }
 
 void launch_trace_rays(const DevScene& S, const float4* rays, uint32_t n, int any_hit, int brute, uint4* hits,

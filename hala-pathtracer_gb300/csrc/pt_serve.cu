@@ -154,6 +154,7 @@ struct pt_server {
   WaveSegment* h_segs = nullptr;  // pinned
   uint32_t seg_cap = 0;
   WaveBuffers W;
+  Buf<uint32_t> errw;  // traversal error word of every job's scene record (TRAV_ERR_* bits)
 
   std::thread admit_thr, render_thr;
 
@@ -334,7 +335,7 @@ bool plan_wave(pt_server* s, std::vector<Segment>& segs, uint32_t cap) {
 
 // Runs one wavefront on the server stream (render thread, no lock held).
 cudaError_t run_wave(pt_server* s, std::vector<Segment>& segs, uint32_t total, uint64_t* launches, bool* timed_out,
-                     uint64_t rays[2], float* ms) {
+                     uint64_t rays[2], float* ms, uint32_t* trav_err) {
   cudaError_t e;
   cudaStream_t st = s->stream;
   const bool med = (segs[0].job->features & PT_FEATURE_MEDIUM) != 0;
@@ -353,6 +354,7 @@ cudaError_t run_wave(pt_server* s, std::vector<Segment>& segs, uint32_t total, u
     Job& j = *g.job;
     if (j.slot_dirty) {
       s->h_jobs[j.slot] = j.r->view;
+      s->h_jobs[j.slot].err = s->errw.p;
       if ((e = cudaMemcpyAsync(s->d_jobs.p + j.slot, s->h_jobs + j.slot, sizeof(DevScene), cudaMemcpyHostToDevice,
                                st)) != cudaSuccess)
         return e;
@@ -365,6 +367,7 @@ cudaError_t run_wave(pt_server* s, std::vector<Segment>& segs, uint32_t total, u
       cudaSuccess)
     return e;
   if ((e = cudaMemsetAsync(s->W.rays.p, 0, 4 * sizeof(unsigned long long), st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(s->errw.p, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
   if ((e = cudaEventRecord(s->ev0, st)) != cudaSuccess) return e;
   launch_camera_multi(s->W.P, s->d_segs.p, (uint32_t)segs.size(), total, s->W.q_a.p,
                       s->W.counters.p + Q_COUNT + Q_NEXT, st);
@@ -395,9 +398,12 @@ cudaError_t run_wave(pt_server* s, std::vector<Segment>& segs, uint32_t total, u
   if ((e = cudaMemcpyAsync(hr, s->W.rays.p, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st)) !=
       cudaSuccess)
     return e;
+  if ((e = cudaMemcpyAsync(s->pinned + 24, s->errw.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+    return e;
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
   rays[0] = hr[0];
   rays[1] = hr[1];
+  *trav_err = s->pinned[24];
   cudaEventElapsedTime(ms, s->ev0, s->ev1);
   return cudaSuccess;
 }
@@ -438,18 +444,21 @@ void render_loop(pt_server* s) {
     bool timed_out = false;
     uint64_t rays[2] = {0, 0};
     float ms = 0.0f;
-    cudaError_t e = run_wave(s, segs, total, &bounce_launches, &timed_out, rays, &ms);
+    uint32_t trav_err = 0;
+    cudaError_t e = run_wave(s, segs, total, &bounce_launches, &timed_out, rays, &ms, &trav_err);
     lk.lock();
     ++s->st.wavefronts;
-    if (e != cudaSuccess || timed_out) {
+    if (e != cudaSuccess || timed_out || trav_err) {
       const std::string why = e != cudaSuccess ? std::string("CUDA error in a wavefront: ") + cudaGetErrorString(e)
-                                               : std::string("paths still alive after the bounce cap");
+                              : timed_out      ? std::string("paths still alive after the bounce cap")
+                                               : std::string("BVH traversal exceeded its stack or visit limit");
+      const pt_status code = e != cudaSuccess ? PT_ERR_CUDA : timed_out ? PT_ERR_TIMEOUT : PT_ERR_TRAVERSAL;
       for (Segment& g : segs) {
         JobPtr j = g.job;
         auto it = std::find(s->running.begin(), s->running.end(), j);
         if (it != s->running.end()) s->running.erase(it);
         s->resident -= j->est;
-        finish_job(s, j, ST_FAILED, e != cudaSuccess ? PT_ERR_CUDA : PT_ERR_TIMEOUT, why);
+        finish_job(s, j, ST_FAILED, code, why);
         dead.push_back(j);
       }
       continue;
@@ -525,7 +534,7 @@ pt_status pt_server_create(const pt_server_config* cfg, pt_server** out) {
       cudaEventCreate(&s->ev0) != cudaSuccess || cudaEventCreate(&s->ev1) != cudaSuccess ||
       cudaMallocHost(&s->pinned, 256) != cudaSuccess ||
       cudaMallocHost(&s->h_jobs, s->cfg.max_jobs * sizeof(DevScene)) != cudaSuccess ||
-      s->d_jobs.ensure(s->cfg.max_jobs) != cudaSuccess) {
+      s->d_jobs.ensure(s->cfg.max_jobs) != cudaSuccess || s->errw.ensure(1) != cudaSuccess) {
     pt_server_destroy(s);
     return PT_ERR_CUDA;
   }

@@ -178,11 +178,18 @@ __device__ __forceinline__ void cswap(float& ka, int32_t& va, float& kb, int32_t
   }
 }
 
-constexpr int TRAV_STACK = 64;
 constexpr int TRAV4_STACK = 96;  // up to three entries per level of the 4-wide tree
 // Upper bound on node visits of one traversal; a well-formed tree never
 // reaches it, a corrupt one ends the traversal instead of looping.
 constexpr uint32_t TRAV_MAX_VISITS = 1u << 22;
+// Bits of the traversal error word (DevScene::err): a push that found the
+// stack full (a subtree was skipped) and a traversal that hit the visit cap.
+// Either one makes the render call that saw it return PT_ERR_TRAVERSAL.
+constexpr uint32_t TRAV_ERR_STACK = 1u, TRAV_ERR_VISITS = 2u;
+
+static __device__ __noinline__ void trav_error(const DevScene& S, uint32_t bit) {
+  if (S.err) atomicOr(S.err, bit);
+}
 
 // Closest hit over triangles. Returns id == HIT_MISS when nothing is hit.
 struct TravCount {
@@ -212,11 +219,16 @@ __device__ __forceinline__ HitRec trace_tris_closest(const DevScene& S, float3 o
   int32_t st_link[TRAV4_STACK];
   float st_t[TRAV4_STACK];
   int sp = 0;
+  const int lim = (int)min(S.trav_stack, (uint32_t)TRAV4_STACK);
   int32_t cur = 0;  // root is always internal
   uint32_t visits = 0;
+  const uint32_t max_visits = S.trav_visits;
   for (;;) {
     while (cur >= 0) {
-      if (++visits > TRAV_MAX_VISITS || cur == EMPTY_LINK) return h;
+      if (++visits > max_visits || cur == EMPTY_LINK) {
+        trav_error(S, TRAV_ERR_VISITS);
+        return h;
+      }
       if (COUNT) tc->nodes++;
       const float4* nd = S.nodes + 8 * (size_t)cur;
       float tn[4];
@@ -245,9 +257,10 @@ __device__ __forceinline__ HitRec trace_tris_closest(const DevScene& S, float3 o
         if (cur == 0x7FFFFFFF) return h;
         continue;
       }
-      if (nh >= 4 && sp < TRAV4_STACK) { st_link[sp] = v3; st_t[sp] = k3; ++sp; }
-      if (nh >= 3 && sp < TRAV4_STACK) { st_link[sp] = v2; st_t[sp] = k2; ++sp; }
-      if (nh >= 2 && sp < TRAV4_STACK) { st_link[sp] = v1; st_t[sp] = k1; ++sp; }
+      if (sp + nh - 1 > lim) trav_error(S, TRAV_ERR_STACK);  // a far child is dropped below
+      if (nh >= 4 && sp < lim) { st_link[sp] = v3; st_t[sp] = k3; ++sp; }
+      if (nh >= 3 && sp < lim) { st_link[sp] = v2; st_t[sp] = k2; ++sp; }
+      if (nh >= 2 && sp < lim) { st_link[sp] = v1; st_t[sp] = k1; ++sp; }
       cur = v0;
     }
     // leaf
@@ -287,11 +300,16 @@ __device__ __forceinline__ bool trace_tris_any(const DevScene& S, float3 o, floa
   const SlabRay sr = slab_ray(o, d);
   int32_t stack[TRAV4_STACK];
   int sp = 0;
+  const int lim = (int)min(S.trav_stack, (uint32_t)TRAV4_STACK);
   int32_t cur = 0;
   uint32_t visits = 0;
+  const uint32_t max_visits = S.trav_visits;
   for (;;) {
     while (cur >= 0) {
-      if (++visits > TRAV_MAX_VISITS || cur == EMPTY_LINK) return false;
+      if (++visits > max_visits || cur == EMPTY_LINK) {
+        trav_error(S, TRAV_ERR_VISITS);
+        return false;
+      }
       const float4* nd = S.nodes + 8 * (size_t)cur;
       float tn[4];
       bool hit[4];
@@ -303,7 +321,8 @@ __device__ __forceinline__ bool trace_tris_any(const DevScene& S, float3 o, floa
       for (int k = 0; k < 4; ++k) {
         if (!hit[k]) continue;
         if (next == 0x7FFFFFFF) next = L[k];
-        else if (sp < TRAV4_STACK) stack[sp++] = L[k];
+        else if (sp < lim) stack[sp++] = L[k];
+        else trav_error(S, TRAV_ERR_STACK);
       }
       if (next == 0x7FFFFFFF) {
         if (sp == 0) return false;

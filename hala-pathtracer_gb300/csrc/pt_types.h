@@ -101,6 +101,10 @@ struct DevScene {
   const float4* tex_texels;
   const uint4* tex_info;
   uint32_t num_textures;
+  // traversal limits (stack entries <= 96, node visits per ray) and the
+  // device word their violations are reported in (TRAV_ERR_* bits)
+  uint32_t trav_stack, trav_visits;
+  uint32_t* err;
 };
 
 // Structure-of-arrays path state of one wavefront (capacity P paths).

@@ -65,7 +65,10 @@ typedef enum pt_status {
   PT_ERR_NOT_READY = 5,
   PT_ERR_UNSUPPORTED = 6,
   PT_ERR_STATE = 7,
-  PT_ERR_CANCELLED = 8
+  PT_ERR_CANCELLED = 8,
+  PT_ERR_TRAVERSAL = 9  /* a BVH traversal ran out of stack or hit its visit cap: the
+                           images of that call may be wrong (no reference counterpart:
+                           RT-core traversal has no such limit) */
 } pt_status;
 
 /* Camera, inc/types.glsl:2-11. `type` 0 = perspective, 1 = orthographic. */
@@ -177,7 +180,9 @@ typedef struct pt_tracer_config {
   int32_t use_simple_aces;
   uint32_t seed;
   uint64_t max_samples;   /* 0 = unlimited */
-  uint32_t wave_paths;    /* paths in flight per wavefront; 0 = 1 << 27 (about 35 GB) */
+  uint32_t wave_paths;    /* paths in flight per wavefront; 0 = as many as half the free device
+                             memory holds at the first render, at most 1 << 27 (about 35 GB),
+                             halved again while the allocation fails */
   uint32_t keep_samples;  /* 1 = keep per-path radiance and hit-sequence hash of the last render call */
 } pt_tracer_config;
 
@@ -210,6 +215,8 @@ typedef struct pt_stats {
   uint64_t cache_train_samples;  /* training samples gathered, last render call */
   uint64_t cache_train_steps;    /* optimiser steps, last render call */
   double cache_loss;             /* loss of the last training batch */
+  uint64_t wave_paths;           /* wavefront capacity (paths) of the last render call */
+  uint64_t bvh_binary_nodes;     /* nodes of the binary tree before the 4-wide collapse */
 } pt_stats;
 
 /* Profiling switches for pt_renderer_set_profiling. */
@@ -299,6 +306,24 @@ pt_status pt_renderer_get_stream(const pt_renderer* r, void** stream);
 pt_status pt_renderer_trace_rays(pt_renderer* r, const float* rays, uint32_t n,
                                  int32_t any_hit, int32_t brute_force, uint32_t* hits);
 
+/* Traversal limits of this renderer: stack entries per ray (1..96; 0 = 96)
+ * and node visits per ray (0 = 2^22). A traversal that needs more stack than
+ * `stack_entries` skips a subtree, and one that reaches `max_visits` stops;
+ * either sets a device error word that the render call (or trace_rays) that
+ * saw it turns into PT_ERR_TRAVERSAL. The defaults are never reached by a
+ * tree the library builds; smaller values exist to exercise that report.
+ * No counterpart in the reference (RT-core traversal has no user limits). */
+pt_status pt_renderer_set_traversal_limits(pt_renderer* r, uint32_t stack_entries, uint32_t max_visits);
+
+/* Per-path results of the last render call for selected paths, gathered on
+ * the device (keep_samples must be on). paths: n indices k into that call's
+ * paths (k = frame_local * width * height + pixel); radiance: 3 floats per
+ * path; hash: the hit-sequence hash (either output may be NULL). The same
+ * values PT_IMAGE_SAMPLE_RADIANCE / PT_IMAGE_SAMPLE_HASH return for those
+ * paths, without copying all of them. No counterpart in the reference. */
+pt_status pt_renderer_read_samples(pt_renderer* r, const uint64_t* paths, uint32_t n, float* radiance,
+                                   uint32_t* hash);
+
 /* ---- allocation-free BVH rebuild ------------------------------------------
  * No counterpart in the reference (its acceleration structures are built by
  * the Vulkan driver inside hala-renderer). Some callers may not call
@@ -317,13 +342,31 @@ pt_status pt_renderer_trace_rays(pt_renderer* r, const float* rays, uint32_t n,
  *   stream          cudaStream_t (NULL = default stream)
  *   error_message   optional host buffer for the reason of a failure
  *
+ * Output layout: a binary tree, node 0 the root, 64 bytes (4 float4) per node:
+ *   q0 = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)   child 0's box, x and y
+ *   q1 = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)   child 1's box, x and y
+ *   q2 = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)   both boxes, z
+ *   q3 = (link0, link1, 0, 0) as int32: link >= 0 is an internal node index;
+ *        link < 0 is a leaf of the triangles tri_sorted_out[start .. start +
+ *        count), start = link & 0x03FFFFFF, count = (link >> 26) & 0x1F.
+ * The boxes are widened by a few ulps so a slab test in float32 never misses
+ * a triangle inside them. The tree is the one pt_renderer_commit builds for
+ * the same triangles (same binned-SAH splits, same node count, same leaf
+ * order); the renderer traverses its 4-wide collapse, which it builds itself,
+ * so this output is for the caller's own traversal kernels (a pt_renderer
+ * does not take an external BVH).
+ *
  * Limits: at most PT_NOALLOC_MAX_TRIANGLES triangles (larger inputs return
  * PT_ERR_INVALID_ARG with that reason); the scratch (about 11.3 MB) stays
  * resident on every device that loads the library until the process exits.
- * It calls no cudaMalloc/cudaFree. Its first call on a device looks up the
- * scratch array's device address (cudaGetSymbolAddress); make that first call
- * before any stream capture. All calls share the one array: calls that overlap
- * on the GPU (other streams, other threads) race and must be serialised. */
+ * It calls no cudaMalloc/cudaFree. The first call in a device's context looks
+ * up the scratch array's device address (cudaGetSymbolAddress, repeated after
+ * cudaDeviceReset gives the device a new context); make that first call
+ * before any stream capture. The build runs level by level and reads each
+ * level's task count back to the host: the call synchronises `stream` once per
+ * tree level and returns when the build is complete. All calls share the one
+ * array: calls that overlap on the GPU (other streams, other threads) race and
+ * must be serialised. */
 #define PT_NOALLOC_MAX_TRIANGLES 65536u
 pt_status pt_bvh_build_noalloc(const void* tri_v0, const void* tri_e1, const void* tri_e2,
                                uint32_t num_triangles, void* nodes_out, uint32_t node_capacity,

@@ -132,7 +132,10 @@ class Oracle:
         L.or_set_sky_color(self.h, s)
         L.or_set_env_intensity(self.h, scene.env_intensity)
         L.or_set_exposure_value(self.h, scene.exposure_value)
+        import time
+        t0 = time.perf_counter()
         rc = L.or_commit(self.h)
+        self.commit_s = time.perf_counter() - t0  # CPU BVH build (+ environment tables)
         if rc != 0:
             raise ValueError(f"or_commit failed: {rc}")
         self.width, self.height = self.cfg.width, self.cfg.height
@@ -189,3 +192,15 @@ class Oracle:
         a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
         lib().or_counters(self.h, C.byref(a), C.byref(b), C.byref(c))
         return a.value, b.value, c.value
+
+
+def running_mean(rad):
+    """Accumulated pixels of (frames, pixels, 3) float32 per-path radiance in
+    frame order, the way pathtracer.rgen.glsl:259-278 accumulates: frame 0
+    stored, then mix(a, x, 1 / (f + 1)) in float32, each operation rounded."""
+    a = np.array(rad[0], np.float32, copy=True)
+    one = np.float32(1.0)
+    for f in range(1, rad.shape[0]):
+        t = one / (np.float32(f) + one)
+        a = a * (one - t) + rad[f] * t
+    return a

@@ -35,7 +35,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(os.path.dirname(HERE), "_ref")
-DEFAULT_SRC = "/root/reference/shaders/src"
+DEFAULT_SRC = os.path.join(os.environ.get("HALA_REFERENCE", "/root/reference"), "shaders", "src")
 
 SHADERS = [
     "hala-pathtracer/pathtracer.rgen.glsl",

@@ -11,7 +11,7 @@ import zlib
 import numpy as np
 import pytest
 
-REF_ASSETS = "/root/reference/assets"
+REF_ASSETS = os.path.join(os.environ.get("HALA_REFERENCE", "/root/reference"), "assets")
 
 
 @pytest.fixture(scope="module")
@@ -298,24 +298,26 @@ def test_config_paths_resolve_like_the_reference(pt, tmp_path, monkeypatch):
     assert cli.resolve("./assets/x.gltf", str(conf)) == os.path.join(str(tmp_path), "./assets/x.gltf")
 
 
-@pytest.mark.gpu
-def test_cli_renders_a_yaml_config(pt, gltf, exr, png, tmp_path):
-    """The reference's YAML schema end to end: glTF scene + EXR HDRI through
-    the CLI, images written; the result equals renderer_for on the same
-    scene (the loaders feed the same renderer calls)."""
-    from tests.golden import pin_scenes
-    s = pin_scenes.disney_ibl()
-    gltf.save_scene(s, str(tmp_path / "scene"))
-    exr.write(str(tmp_path / "sky.exr"), s.env_rgb)
-    (tmp_path / "c.yaml").write_text(
-        "window:\n  width: 32\n  height: 18\ntracer:\n  max_depth: 12\n  rr_depth: 4\n  exposure_value: -1.0\n"
-        "  tonemap:\n    enable: true\n    enable_aces: true\n    use_simple_aces: false\n  max_samples: 2\n"
-        "scene_file: ./scene.gltf\nhdri_file: ./sky.exr\nhdri_rotation: 77.8\n"
-        "ground_color: [0.0, 0.0, 0.0]\nsky_color: [0.0, 0.0, 0.0]\n")
-    cli = importlib.import_module("hala-pathtracer_gb300.cli")
-    out = str(tmp_path / "img")
-    assert cli.main(["-c", str(tmp_path / "c.yaml"), "--out", out]) == 0
-    for suffix in ("_color.pfm", "_albedo.pfm", "_normal.pfm", "_final.ppm", "_final.png"):
-        assert os.path.getsize(out + suffix) > 0
-    final = png.read(out + "_final.png")
-    assert final.shape == (18, 32, 4) and final[..., :3].max() > 0
+# ----------------------------------------------------------------- PFM
+
+def test_pfm_round_trip_and_layout(pt, tmp_path):
+    """Rows are stored bottom to top, little-endian with a negative scale."""
+    pfm = importlib.import_module("hala-pathtracer_gb300.pfm")
+    rng = np.random.default_rng(4)
+    img = rng.normal(size=(7, 11, 3)).astype(np.float32)
+    img[0, 0] = [np.inf, -0.0, np.nan]
+    p = str(tmp_path / "a.pfm")
+    pfm.write(p, img)
+    raw = open(p, "rb").read()
+    assert raw.startswith(b"PF\n11 7\n-1.0\n")
+    body = np.frombuffer(raw[len(b"PF\n11 7\n-1.0\n"):], "<f4").reshape(7, 11, 3)
+    assert np.array_equal(body[-1].view(np.uint32), img[0].view(np.uint32))  # top row stored last
+    back = pfm.read(p)
+    assert np.array_equal(back.view(np.uint32), img.view(np.uint32))
+    # big-endian files (positive scale) read too
+    big = b"PF\n11 7\n1.0\n" + np.ascontiguousarray(img[::-1]).astype(">f4").tobytes()
+    assert np.array_equal(pfm.read(big).view(np.uint32), img.view(np.uint32))
+    with pytest.raises(pfm.PfmError):
+        pfm.read(b"P6\n1 1\n255\n\0\0\0")
+    with pytest.raises(pfm.PfmError):
+        pfm.read(raw[:-4])

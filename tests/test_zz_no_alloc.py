@@ -5,13 +5,17 @@ their device pools at start-up and rebuild the BVH of animated geometry every
 frame inside that budget. pt_bvh_build_noalloc serves them by building into
 caller-owned buffers, with its scratch in a fixed library-owned device array.
 
-The test builds the BVH of one scene through that entry point twice in a row
-and checks each result against the library's ordinary build (the one
-pt_renderer_commit runs): the same node count, the triangles in leaf order
-are a permutation of the input, and the closest hit of every test ray found
-by walking the returned nodes is bit-identical (t, u, v, triangle id) to
-pt_renderer_trace_rays on the committed renderer. It also checks that an
-input above the limit is refused with a reason.
+The tests build the BVH of a scene through that entry point twice in a row
+and check each result against the library's ordinary build (the one
+pt_renderer_commit runs): the same binary node count, the triangles in leaf
+order a permutation of the input, and the closest hit of every test ray
+found by walking the returned nodes bit-identical (t, u, v, triangle id) to
+pt_renderer_trace_rays on the committed renderer. Scenes: a small icosphere
+(under the ordinary build's multi-block threshold) and a soup of exactly
+PT_NOALLOC_MAX_TRIANGLES = 65,536 triangles (the largest input, where the
+ordinary build splits the top levels with all blocks and the allocation-free
+one with one block per task). The device's free memory is the same before
+and after the second call. An input above the limit is refused with a reason.
 """
 import ctypes as C
 
@@ -122,35 +126,56 @@ def _closest(nodes, tris, o, d, tmin, tmax):
                     np.uint32)
 
 
-def test_noalloc_bvh_matches_renderer_build(pt, scenes):
+def _soup(scenes, n, seed):
+    """n small random triangles in the unit cube, one material, a camera."""
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(0.0, 1.0, size=(n, 1, 3))
+    pos = (c + rng.uniform(-0.02, 0.02, size=(n, 3, 3))).reshape(-1, 3)
+    z = np.zeros((3 * n, 3))
+    s = scenes.Scene("soup")
+    m = s.add_material(scenes.material())
+    s.add_mesh(scenes.pack_vertices(pos, z + [0, 0, 1], z + [1, 0, 0], np.zeros((3 * n, 2))),
+               np.arange(3 * n, dtype=np.uint32), m)
+    s.cameras.append(scenes.look_at((0.5, -2.0, 0.5), (0.5, 0.5, 0.5), 40.0))
+    s.width, s.height, s.spp = 16, 16, 1
+    return s
+
+
+def _check_noalloc_build(pt, sc, nrays, seed):
     torch = pytest.importorskip("torch")
     pt.build()
     lib = pt.load_library()
-    sc = scenes.tiny_variants()["icosphere"]
     sc.lights = []  # triangles only: the walk below does not include analytic lights
     r = pt.renderer_for(sc)
     n = sc.num_triangles
-    rng = np.random.default_rng(21)
+    binary_nodes = r.stats().bvh_binary_nodes
+    rng = np.random.default_rng(seed)
     pts = np.concatenate([m[0][:, :3] for m in sc.meshes])
-    rays = np.zeros((256, 8), np.float32)
-    rays[:, 0:3] = rng.uniform(pts.min(0), pts.max(0), size=(256, 3))
-    dirs = rng.normal(size=(256, 3))
+    rays = np.zeros((nrays, 8), np.float32)
+    rays[:, 0:3] = rng.uniform(pts.min(0), pts.max(0), size=(nrays, 3))
+    dirs = rng.normal(size=(nrays, 3))
     rays[:, 4:7] = dirs / np.linalg.norm(dirs, axis=1, keepdims=True)
     rays[:, 7] = 1e4
     expected = r.trace_rays(rays)
+    r.close()
 
     v0, e1, e2 = (torch.from_numpy(a).cuda() for a in _world_triangles(sc))
+    nodes = torch.empty((4 * 2 * n, 4), device="cuda")
+    tri_sorted = torch.empty((3 * n, 4), device="cuda")
     for call in range(2):
-        nodes = torch.full((4 * 2 * n, 4), float("nan"), device="cuda")
-        tri_sorted = torch.full((3 * n, 4), float("nan"), device="cuda")
+        nodes.fill_(float("nan"))
+        tri_sorted.fill_(float("nan"))
         nn = C.c_uint32(0)
         err = C.create_string_buffer(256)
         torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
         st = lib.pt_bvh_build_noalloc(v0.data_ptr(), e1.data_ptr(), e2.data_ptr(), n, nodes.data_ptr(), 2 * n,
                                       tri_sorted.data_ptr(), C.byref(nn), None, err, 256)
         torch.cuda.synchronize()
         assert st == 0, err.value.decode()
-        assert 0 < nn.value <= 2 * n  # binary nodes (the renderer traverses their 4-wide collapse)
+        if call == 1:
+            assert torch.cuda.mem_get_info()[0] == free_before, "device memory changed during the call"
+        assert nn.value == binary_nodes, (nn.value, binary_nodes)
         hn = nodes[:4 * nn.value].cpu().numpy()
         ht = tri_sorted.cpu().numpy()
         ids = ht[0::3, 3].view(np.uint32)
@@ -158,6 +183,17 @@ def test_noalloc_bvh_matches_renderer_build(pt, scenes):
         got = np.stack([_closest(hn, ht, rays[k, 0:3], rays[k, 4:7], f32(rays[k, 3]), f32(rays[k, 7]))
                         for k in range(len(rays))])
         assert np.array_equal(got, expected), f"call {call}: {(got != expected).any(1).sum()} rays differ"
+        assert (expected[:, 3] != MISS).any()
+
+
+def test_noalloc_bvh_matches_renderer_build(pt, scenes):
+    _check_noalloc_build(pt, scenes.tiny_variants()["icosphere"], 256, 21)
+
+
+def test_noalloc_bvh_at_the_size_limit(pt, scenes):
+    sc = _soup(scenes, pt.abi.NOALLOC_MAX_TRIANGLES, 5)
+    assert sc.num_triangles == 65536
+    _check_noalloc_build(pt, sc, 96, 22)
 
 
 def test_noalloc_bvh_rejects_oversized_input(pt):
