@@ -19,8 +19,11 @@ host-driven bounce loop; events cannot sit inside the graph).
 --impl reference times the CPU restatement of the reference integrator on
 the host cores over a bounded sample of the same workload.
 
-Multi-GPU: every rank renders its own full workload with a distinct sample
-range (independent units, no data-path collective): scaling "weak".
+Multi-GPU: every rank renders the full workload's pixels for its own range of
+frames (rank r: frames r * spp .. (r + 1) * spp - 1 of one render), so N
+ranks render one image of N * spp samples; the accumulators are merged once
+after the timed steps (partition.merge_accumulation, one all-reduce).
+Per-rank work is fixed as N grows: scaling "weak".
 """
 import argparse
 import importlib
@@ -57,10 +60,11 @@ def _dist():
     return ws, rank, local
 
 
-def rank_seed(seed, rank):
-    """Per-rank RNG seed offset: every rank renders its own sample range of
-    the workload (independent units, no data-path collective)."""
-    return seed + rank * 100003
+def rank_seed(seed, rank, frames):
+    """RNG seed of a rank: the seed is added to the frame index, so rank r
+    renders frames [r * frames, (r + 1) * frames) of one render of
+    world * frames frames (partition.frame_range with equal blocks)."""
+    return seed + rank * frames
 
 
 def max_over_ranks(x, device="cuda"):
@@ -184,12 +188,16 @@ def cpu_baseline(scene, seconds=12.0, threads=0, gpu_accum=None):
            "sample": f"{npix} seeded random pixels x all {scene.spp} frames of the full workload ({dt:.1f} s)"}
     if gpu_accum is not None:
         ref = oracle.running_mean(rad)
-        got = gpu_accum.reshape(-1, 4)[pix.astype(np.int64), :3]
-        same = (got.view(np.uint32) == ref.view(np.uint32)).all(1)
+        got = np.ascontiguousarray(gpu_accum.reshape(-1, 4)[pix.astype(np.int64), :3])
+        # bit for bit; a NaN equals a NaN (the payload of a NaN differs between CPU and GPU)
+        same = ((got.view(np.uint32) == ref.view(np.uint32)) | (np.isnan(got) & np.isnan(ref))).all(1)
+        bad = np.nonzero(~same)[0]
         out["parity"] = {"pixels_checked": int(npix), "paths_covered": int(npix * scene.spp),
-                         "mismatched_pixels": int((~same).sum()),
+                         "mismatched_pixels": int(len(bad)), "nan_pixels": int(np.isnan(ref).any(1).sum()),
+                         "first_mismatches": [{"pixel": int(pix[k]), "gpu": got[k].tolist(), "oracle": ref[k].tolist()}
+                                              for k in bad[:4]],
                          "check": "accumulated pixels of the last timed GPU render against the oracle's running "
-                                  "mean of the same pixels' paths, bit for bit"}
+                                  "mean of the same pixels' paths, bit for bit (NaN equals NaN)"}
     return out
 
 
@@ -484,7 +492,7 @@ def main():
     abi = pt.abi
     pt.build()
 
-    scene.seed = rank_seed(scene.seed, rank)  # distinct sample range per rank
+    scene.seed = rank_seed(scene.seed, rank, scene.spp)  # this rank's frames of the job
     r = pt.renderer_for(scene)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
@@ -533,6 +541,22 @@ def main():
     paths_step = scene.width * scene.height * scene.spp
     value = ws * paths_step * args.steps / (total_ms / 1e3)
     rays_per_s = ws * (closest + shadow) / (total_ms / 1e3)
+
+    merge = None
+    if ws > 1:
+        # the job's one collective: the frame-weighted mean of the ranks'
+        # accumulators (an all-reduce of W x H x 4 floats per image)
+        part = importlib.import_module("hala-pathtracer_gb300.partition")
+        imgs = [torch.empty((scene.height, scene.width, 4), dtype=torch.float32, device="cuda") for _ in range(3)]
+        for which, t in zip((abi.IMAGE_ACCUM, abi.IMAGE_ALBEDO, abi.IMAGE_NORMAL), imgs):
+            r.image_into(which, t.data_ptr(), t.numel() * 4)
+        barrier()
+        t0 = time.perf_counter()
+        merged, total_frames = part.merge_accumulation(imgs, scene.spp)
+        torch.cuda.synchronize()
+        merge = {"frames_total": total_frames, "ms": 1e3 * (time.perf_counter() - t0),
+                 "bytes_per_rank": 3 * imgs[0].numel() * 4}
+        del merged
 
     # the same steps again with CUDA events around every closest-hit launch
     # (host-driven bounce loop: events cannot sit inside the bounce graph)
@@ -611,6 +635,8 @@ def main():
         "gpu_launches": launches,
         "clocks": clk,
     }
+    if merge is not None:
+        line["merge"] = merge
     if rank == 0 and not args.no_cpu_baseline:
         try:
             cb = cpu_baseline(scene, gpu_accum=timed_accum)

@@ -99,6 +99,12 @@ class Renderer:
         self._check(self._lib.pt_renderer_set_envmap(self._h, a.ctypes.data_as(C.POINTER(C.c_float)),
                                                      a.shape[1], a.shape[0], float(rotation_degrees)))
 
+    def set_envmap_file(self, path, rotation_degrees=0.0):
+        """HalaRenderer::set_envmap(&hdri_file, rotation): the OpenEXR file read
+        by the library itself (pt_renderer_set_envmap_file)."""
+        self._check(self._lib.pt_renderer_set_envmap_file(self._h, None if path is None else str(path).encode(),
+                                                          float(rotation_degrees)))
+
     def set_ground_color(self, rgba):
         self._check(self._lib.pt_renderer_set_ground_color(self._h, _f4(rgba)))
 
@@ -150,6 +156,17 @@ class Renderer:
             out = np.empty((self.height, self.width, 4), np.float32)
         self._check(self._lib.pt_renderer_read_image(self._h, which, out.ctypes.data, out.nbytes))
         return out
+
+    def image_into(self, which, ptr, nbytes):
+        """Copies one image into memory at address `ptr` (host, or device
+        memory of the renderer's device, e.g. a torch tensor's data_ptr())."""
+        self._check(self._lib.pt_renderer_read_image(self._h, which, C.c_void_p(ptr), int(nbytes)))
+
+    def load_accumulation_ptr(self, accum_ptr, albedo_ptr, normal_ptr, frame_index):
+        """load_accumulation from raw addresses (host or device memory), each
+        W * H float4."""
+        self._check(self._lib.pt_renderer_load_accumulation(self._h, C.c_void_p(accum_ptr), C.c_void_p(albedo_ptr),
+                                                            C.c_void_p(normal_ptr), int(frame_index)))
 
     def samples(self):
         """Per-path radiance (n, 3) and hit-sequence hash (n,) of the last render
@@ -221,6 +238,22 @@ def renderer_for(scene, **cfg_over):
     r.set_exposure_value(scene.exposure_value)
     r.commit()
     return r
+
+
+def read_exr(path):
+    """(H, W, 3) float32 pixels of an OpenEXR file through the library's own
+    reader (pt_exr_read_rgb)."""
+    lib = load_library()
+    w, h = C.c_uint32(), C.c_uint32()
+    err = C.create_string_buffer(256)
+    st = lib.pt_exr_read_rgb(str(path).encode(), None, 0, C.byref(w), C.byref(h), err, 256)
+    if st != abi.PT_OK:
+        raise PTError(st, err.value.decode())
+    out = np.empty((h.value, w.value, 3), np.float32)
+    st = lib.pt_exr_read_rgb(str(path).encode(), out.ctypes.data, out.size, C.byref(w), C.byref(h), err, 256)
+    if st != abi.PT_OK:
+        raise PTError(st, err.value.decode())
+    return out
 
 
 def _cache_config(**kw):

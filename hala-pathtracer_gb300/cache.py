@@ -89,7 +89,7 @@ class RadianceCache:
 
 def main(argv=None):
     """Device-timed cache kernels on seeded records (profiling entry point):
-    python hala-pathtracer_gb300/cache.py --queries N --iterations K"""
+    python -m hala-pathtracer_gb300.cache --queries N --iterations K"""
     import argparse
     ap = argparse.ArgumentParser(description="radiance-cache kernel benchmark")
     ap.add_argument("--queries", type=int, default=1 << 22)
@@ -103,8 +103,5 @@ def main(argv=None):
 
 
 if __name__ == "__main__":
-    import importlib
-    import os
     import sys
-    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
-    sys.exit(importlib.import_module("hala-pathtracer_gb300.cache").main())
+    sys.exit(main())

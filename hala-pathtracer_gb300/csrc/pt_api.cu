@@ -837,11 +837,12 @@ pt_status pt_renderer_commit(pt_renderer* r) {
     if (rc == 2) return fail(r, PT_ERR_OOM, "BVH build: out of device memory");
     if (rc != 0) return fail(r, PT_ERR_CUDA, "BVH build failed (code " + std::to_string(rc) + ")");
     CK(r, r->nodes.ensure(8 * (size_t)std::max<uint32_t>(nn, 1)));
-    rc = collapse_bvh4(bin.p, nn, r->nodes.p, std::max<uint32_t>(nn, 1), &nn4, st);
+    uint32_t leaves = 0;
+    rc = collapse_bvh4(bin.p, nn, r->nodes.p, std::max<uint32_t>(nn, 1), &nn4, st, &leaves);
     if (rc == 2) return fail(r, PT_ERR_OOM, "BVH collapse: out of device memory");
     if (rc != 0) return fail(r, PT_ERR_CUDA, "BVH collapse failed (code " + std::to_string(rc) + ")");
     r->nnodes = nn4;
-    r->stats.bvh_binary_nodes = nn;
+    r->stats.bvh_binary_nodes = 2ull * leaves - 1;  // reachable from the root (the build reserves more slots)
   } else {
     r->stats.bvh_binary_nodes = 0;
     CK(r, r->nodes.ensure(8));
@@ -882,7 +883,8 @@ pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) {
   if (total == 0) return PT_OK;
   const bool med = (r->features & PT_FEATURE_MEDIUM) != 0;
   const bool auto_wave = r->cfg.wave_paths == 0;
-  uint64_t want = auto_wave ? (r->W.cap ? r->W.cap : default_wave_paths(med)) : r->cfg.wave_paths;
+  if (auto_wave && r->auto_wave_paths == 0) r->auto_wave_paths = default_wave_paths(med);
+  uint64_t want = auto_wave ? r->auto_wave_paths : r->cfg.wave_paths;
   if (r->cache_on) want = std::min<uint64_t>(want, r->cache_cfg.paths_per_pass);
   uint32_t cap = (uint32_t)std::min<uint64_t>(want, total);
   for (;;) {
@@ -896,6 +898,7 @@ pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) {
     cudaGetLastError();
     r->W.release();
     cap >>= 1;
+    r->auto_wave_paths = cap;
   }
   if (!r->cache_on) cap = r->W.cap;  // a larger wavefront already allocated costs nothing more
   cudaStream_t st = r->stream;
@@ -1066,9 +1069,9 @@ pt_status pt_renderer_load_accumulation(pt_renderer* r, const float* accum, cons
   if (r->cfg.max_samples > 0 && frame_index > r->cfg.max_samples)
     return fail(r, PT_ERR_INVALID_ARG, "frame_index exceeds max_samples");
   const size_t WH = (size_t)r->cfg.width * r->cfg.height;
-  CK(r, cudaMemcpyAsync(r->accum.p, accum, WH * sizeof(float4), cudaMemcpyHostToDevice, r->stream));
-  CK(r, cudaMemcpyAsync(r->albedo.p, albedo, WH * sizeof(float4), cudaMemcpyHostToDevice, r->stream));
-  CK(r, cudaMemcpyAsync(r->normal.p, normal, WH * sizeof(float4), cudaMemcpyHostToDevice, r->stream));
+  CK(r, cudaMemcpyAsync(r->accum.p, accum, WH * sizeof(float4), cudaMemcpyDefault, r->stream));
+  CK(r, cudaMemcpyAsync(r->albedo.p, albedo, WH * sizeof(float4), cudaMemcpyDefault, r->stream));
+  CK(r, cudaMemcpyAsync(r->normal.p, normal, WH * sizeof(float4), cudaMemcpyDefault, r->stream));
   launch_finalize(r->accum.p, r->final_img.p, (uint32_t)WH, r->exposure, r->cfg.enable_tonemap, r->cfg.enable_aces,
                   r->cfg.use_simple_aces, r->stream);
   CK(r, cudaGetLastError());
@@ -1089,12 +1092,12 @@ pt_status pt_renderer_read_image(pt_renderer* r, pt_image which, void* host, siz
     case PT_IMAGE_NORMAL: {
       if (bytes != WH * sizeof(float4)) return fail(r, PT_ERR_INVALID_ARG, "image size mismatch");
       const float4* src = which == PT_IMAGE_ACCUM ? r->accum.p : (which == PT_IMAGE_ALBEDO ? r->albedo.p : r->normal.p);
-      CK(r, cudaMemcpy(host, src, bytes, cudaMemcpyDeviceToHost));
+      CK(r, cudaMemcpy(host, src, bytes, cudaMemcpyDefault));
       return PT_OK;
     }
     case PT_IMAGE_FINAL:
       if (bytes != WH * 4) return fail(r, PT_ERR_INVALID_ARG, "image size mismatch");
-      CK(r, cudaMemcpy(host, r->final_img.p, bytes, cudaMemcpyDeviceToHost));
+      CK(r, cudaMemcpy(host, r->final_img.p, bytes, cudaMemcpyDefault));
       return PT_OK;
     case PT_IMAGE_SAMPLE_RADIANCE: {
       if (!r->cfg.keep_samples) return fail(r, PT_ERR_STATE, "keep_samples is off");

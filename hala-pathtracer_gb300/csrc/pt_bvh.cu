@@ -950,7 +950,7 @@ __device__ __forceinline__ float bin_child_area(const float4* bin, int32_t node,
 
 __global__ void k_collapse(const float4* bin, const CollapseWork* work, uint32_t nwork, float4* out4,
                            uint32_t* node_counter, uint32_t cap4, CollapseWork* next, uint32_t* next_count,
-                           uint32_t* overflow) {
+                           uint32_t* overflow, uint32_t* leaves) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nwork) return;
   const CollapseWork w = work[i];
@@ -998,6 +998,7 @@ __global__ void k_collapse(const float4* bin, const CollapseWork* work, uint32_t
         q[2 * c + 1][k] = hi[k][c];
       }
       int32_t l = link[k];
+      if (l < 0) atomicAdd(leaves, 1u);
       if (l >= 0) {
         uint32_t slot = atomicAdd(node_counter, 1u);
         if (slot >= cap4) {
@@ -1143,14 +1144,15 @@ int build_bvh(const float4* tri_v0, const float4* tri_e1, const float4* tri_e2, 
   return 0;
 }
 
-int collapse_bvh4(const float4* bin, uint32_t nn_bin, float4* out4, uint32_t cap4, uint32_t* num4, cudaStream_t st) {
+int collapse_bvh4(const float4* bin, uint32_t nn_bin, float4* out4, uint32_t cap4, uint32_t* num4, cudaStream_t st,
+                  uint32_t* num_leaves) {
   if (nn_bin == 0 || cap4 == 0) return 2;
   Tmp<CollapseWork> qa, qb;
-  Tmp<uint32_t> counters;  // [0] 4-wide nodes, [1] next queue A, [2] next queue B, [3] overflow
+  Tmp<uint32_t> counters;  // [0] 4-wide nodes, [1] next queue A, [2] next queue B, [3] overflow, [4] leaves
   const uint32_t qcap = nn_bin + 1;
-  if (qa.alloc(qcap, st) || qb.alloc(qcap, st) || counters.alloc(4, st)) return 2;
+  if (qa.alloc(qcap, st) || qb.alloc(qcap, st) || counters.alloc(5, st)) return 2;
   CollapseWork root{0, 0};
-  uint32_t init[4] = {1, 0, 0, 0};
+  uint32_t init[5] = {1, 0, 0, 0, 0};
   cudaMemcpyAsync(qa.p, &root, sizeof(root), cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(counters.p, init, sizeof(init), cudaMemcpyHostToDevice, st);
   uint32_t nwork = 1, host = 0;
@@ -1160,7 +1162,7 @@ int collapse_bvh4(const float4* bin, uint32_t nn_bin, float4* out4, uint32_t cap
   for (int level = 0; level < 200 && nwork > 0; ++level) {
     cudaMemsetAsync(counters.p + slot, 0, sizeof(uint32_t), st);
     k_collapse<<<(nwork + 255) / 256, 256, 0, st>>>(bin, cur, nwork, out4, counters.p, cap4, nxt, counters.p + slot,
-                                                   counters.p + 3);
+                                                   counters.p + 3, counters.p + 4);
     cudaMemcpyAsync(&host, counters.p + slot, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return 3;
     nwork = host;
@@ -1168,11 +1170,12 @@ int collapse_bvh4(const float4* bin, uint32_t nn_bin, float4* out4, uint32_t cap
     slot = slot == 1 ? 2 : 1;
   }
   if (nwork != 0) return 4;
-  uint32_t res[4];
+  uint32_t res[5];
   cudaMemcpyAsync(res, counters.p, sizeof(res), cudaMemcpyDeviceToHost, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return 3;
   if (res[3] != 0) return 5;
   *num4 = res[0];
+  if (num_leaves) *num_leaves = res[4];
   return 0;
 }
 

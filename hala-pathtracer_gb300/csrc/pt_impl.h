@@ -177,6 +177,7 @@ struct pt_renderer {
 
   // wavefront
   hpt::WaveBuffers W;
+  uint32_t auto_wave_paths = 0;  // default wavefront size, chosen at the first render (wave_paths = 0)
 
   // images
   hpt::Buf<float4> accum, albedo, normal;

@@ -216,7 +216,7 @@ typedef struct pt_stats {
   uint64_t cache_train_steps;    /* optimiser steps, last render call */
   double cache_loss;             /* loss of the last training batch */
   uint64_t wave_paths;           /* wavefront capacity (paths) of the last render call */
-  uint64_t bvh_binary_nodes;     /* nodes of the binary tree before the 4-wide collapse */
+  uint64_t bvh_binary_nodes;     /* nodes of the binary tree (2 x leaves - 1) before the 4-wide collapse */
 } pt_stats;
 
 /* Profiling switches for pt_renderer_set_profiling. */
@@ -250,6 +250,19 @@ pt_status pt_renderer_set_scene(pt_renderer* r, const pt_scene_desc* scene);
  * RGB32F pixels (row 0 = theta 0) and the hdri_rotation in degrees. */
 pt_status pt_renderer_set_envmap(pt_renderer* r, const float* rgb, uint32_t width,
                                  uint32_t height, float rotation_degrees);
+/* HalaRenderer::set_envmap(&hdri_file, rotation) (src/bin/hala-pathtracer.rs:203)
+ * with the file itself: reads an OpenEXR image (single-part scanline; HALF,
+ * FLOAT or UINT channels; NONE, RLE, ZIPS or ZIP compression; R, G, B or a
+ * single Y channel) and calls pt_renderer_set_envmap with its pixels. NULL
+ * clears the map like pt_renderer_set_envmap(r, NULL, ...). Unsupported or
+ * corrupt files return PT_ERR_INVALID_ARG with the reason. */
+pt_status pt_renderer_set_envmap_file(pt_renderer* r, const char* path, float rotation_degrees);
+/* The OpenEXR reader behind pt_renderer_set_envmap_file: RGB float triples,
+ * row 0 at the top. With rgb = NULL only *width and *height are set;
+ * otherwise rgb must hold width * height * 3 floats. No counterpart in the
+ * reference (its exr crate dependency, Cargo.lock:502-504). */
+pt_status pt_exr_read_rgb(const char* path, float* rgb, size_t capacity_floats, uint32_t* width,
+                          uint32_t* height, char* error_message, size_t error_capacity);
 /* HalaRenderer::set_ground_color / set_sky_color (src/bin/hala-pathtracer.rs:205-206). */
 pt_status pt_renderer_set_ground_color(pt_renderer* r, const float rgba[4]);
 pt_status pt_renderer_set_sky_color(pt_renderer* r, const float rgba[4]);
@@ -275,12 +288,15 @@ pt_status pt_renderer_reset(pt_renderer* r);
  * (pt_stats.frame_index). The random sequence of a pixel depends only on the
  * pixel and the frame, so frames rendered afterwards continue exactly where
  * the saved render stopped: the result is bit-identical to an uninterrupted
- * render. The final image is recomputed from accum. No counterpart in the
- * reference, whose accumulation lives only in GPU images. */
+ * render. The final image is recomputed from accum. The three pointers may
+ * be host memory or device memory of the renderer's device. No counterpart in
+ * the reference, whose accumulation lives only in GPU images. */
 pt_status pt_renderer_load_accumulation(pt_renderer* r, const float* accum, const float* albedo,
                                         const float* normal, uint64_t frame_index);
-/* Device->host copy of one image (the data HalaRenderer::save_images writes,
- * src/bin/hala-pathtracer.rs:251). `bytes` must equal the image size. */
+/* Copy of one image (the data HalaRenderer::save_images writes,
+ * src/bin/hala-pathtracer.rs:251). `bytes` must equal the image size. For the
+ * accum, albedo, normal and final images `host` may also be device memory of
+ * the renderer's device (the copy direction follows unified addressing). */
 pt_status pt_renderer_read_image(pt_renderer* r, pt_image which, void* host, size_t bytes);
 /* HalaRenderer::save_images (src/bin/hala-pathtracer.rs:251): writes
  * <prefix>_color.pfm, <prefix>_albedo.pfm, <prefix>_normal.pfm (the files

@@ -20,6 +20,13 @@ pytestmark = pytest.mark.gpu
 PIXELS = 4096
 
 
+def bit_equal(a, b):
+    """Element-wise: the same float32 bits, or both NaN (a path whose
+    throughput turns non-finite gives NaN on both sides, as the reference
+    does, but the NaN's payload differs between the CPU and the GPU)."""
+    return (a.view(np.uint32) == b.view(np.uint32)) | (np.isnan(a) & np.isnan(b))
+
+
 def check_workload(pt, oracle_mod, sc, seed):
     WH = sc.width * sc.height
     r = pt.renderer_for(sc, keep_samples=1)
@@ -37,10 +44,10 @@ def check_workload(pt, oracle_mod, sc, seed):
     hash_o = hash_o.reshape(-1)
     bad = np.nonzero(hash_g != hash_o)[0]
     assert len(bad) == 0, f"{len(bad)} of {len(paths)} hit sequences differ, first path {paths[bad[0]]}"
-    same = (rad_g.view(np.uint32) == rad_o.view(np.uint32)).all(1)
+    same = bit_equal(rad_g, rad_o).all(1)
     assert same.all(), f"{(~same).sum()} of {len(paths)} per-path radiances differ"
     ref = oracle_mod.running_mean(rad_o.reshape(sc.spp, PIXELS, 3))
-    assert np.array_equal(acc.view(np.uint32), ref.view(np.uint32)), "accumulated pixels differ"
+    assert bit_equal(np.ascontiguousarray(acc), ref).all(), "accumulated pixels differ"
     return st
 
 

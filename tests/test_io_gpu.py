@@ -183,7 +183,8 @@ def test_cli_output_equals_the_renderer_images(pt, io, tmp_path):
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), suffix
     final = r.image(3)[..., :3]
     assert final.max() > 0
-    assert np.array_equal(io["png"].read(out + "_final.png")[..., :3], final)
+    png8 = np.round(io["png"].read(out + "_final.png")[..., :3] * 255.0).astype(np.uint8)  # read() gives [0, 1]
+    assert np.array_equal(png8, final)
     assert np.array_equal(_read_ppm(out + "_final.ppm"), final)
     # and the scene is the one written: the same images as the in-memory scene
     s2 = pin_scenes.disney_ibl()
@@ -201,3 +202,26 @@ def test_reference_cornell_gltf_on_the_gpu(pt, io, oracle_mod):
     s = io["gltf"].load_scene(os.path.join(REF_ASSETS, "cornell-box.gltf"), 40, 30)
     s.spp, s.max_depth, s.rr_depth = 3, 8, 4
     same_as_oracle(pt, oracle_mod, s)
+
+
+def test_envmap_file_entry_point(pt, io, tmp_path):
+    """pt_renderer_set_envmap_file (the library's own EXR reader, for hosts
+    without a Python loader) gives the images of set_envmap with exr.py's
+    pixels, bit for bit; a file it cannot read is refused with the reason."""
+    from tests.golden import pin_scenes
+    s = pin_scenes.disney_ibl()
+    p = str(tmp_path / "sky.exr")
+    io["exr"].write(p, s.env_rgb, half=True, compression="ZIP")
+    a = pt.renderer_for(s)
+    a.set_envmap_file(p, s.env_rotation_deg)
+    a.commit()
+    a.render(2)
+    s.env_rgb = io["exr"].read_rgb(p)
+    b = pt.renderer_for(s)
+    b.render(2)
+    for k in (0, 1, 2, 3):
+        assert np.array_equal(a.image(k).view(np.uint8), b.image(k).view(np.uint8)), k
+    bad = tmp_path / "bad.exr"
+    bad.write_bytes(b"not an exr")
+    with pytest.raises(pt.PTError, match="not an OpenEXR"):
+        a.set_envmap_file(str(bad), 0.0)

@@ -80,6 +80,8 @@ def test_default_wavefront_is_sized_from_free_memory(pt, scenes):
     r.render(4)
     w = r.stats().wave_paths
     assert w == 64 * 64 * 4  # the render is smaller than any default wavefront
+    r.render(60)  # a larger call is not held to the first call's size
+    assert r.stats().wave_paths == 64 * 64 * 60
     big = scenes.cornell(1024, 1024, 64)
     r2 = pt.renderer_for(big, wave_paths=0)
     r2.render(64)

@@ -1,6 +1,6 @@
-"""The N > 1 bench path on the host: each rank renders its own sample range
-(distinct RNG seeds) and the job's time is the slowest rank's. Two gloo ranks
-on the CPU; no GPU involved."""
+"""The N > 1 bench path on the host: each rank renders its own frame range of
+one render (seed offset by the frames before it) and the job's time is the
+slowest rank's. Two gloo ranks on the CPU; no GPU involved."""
 import os
 import socket
 
@@ -20,7 +20,7 @@ def _worker(rank, world, port, out):
     dist.init_process_group("gloo", rank=rank, world_size=world)
     import bench
     t = bench.max_over_ranks(10.0 + 7.5 * rank, device="cpu")
-    out[rank] = (bench.rank_seed(1, rank), t)
+    out[rank] = (bench.rank_seed(1, rank, 64), t)
     dist.barrier()
     dist.destroy_process_group()
 
@@ -32,11 +32,11 @@ def test_two_gloo_ranks_take_distinct_samples_and_the_slowest_time():
     mp.start_processes(_worker, args=(world, _free_port(), out), nprocs=world, start_method="spawn")
     seeds = [out[r][0] for r in range(world)]
     times = [out[r][1] for r in range(world)]
-    assert len(set(seeds)) == world
+    assert seeds == [1, 65]  # rank 1 starts where rank 0's 64 frames end
     assert times == [17.5, 17.5]
 
 
 def test_single_process_is_its_own_maximum():
     import bench
     assert bench.max_over_ranks(3.25) == 3.25
-    assert bench.rank_seed(5, 0) == 5
+    assert bench.rank_seed(5, 0, 64) == 5
