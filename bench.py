@@ -419,11 +419,13 @@ def radiance_cache_leg(pt, target_spp=256):
     }
 
 
-def serving_leg(n_jobs=256, rate=20.0, seed=0):
+def serving_leg(n_jobs=256, rate=20.0, seed=0, cache=None):
     """The serving mix: `n_jobs` render jobs with Poisson arrivals at `rate`
     jobs/s, scenes drawn from the four workloads with seed-perturbed
     materials and lights, resolution log-uniform 128^2..1920x1080, spp
-    log-uniform 1..256, all through one pt_server."""
+    log-uniform 1..256, all through one pt_server. With `cache` (a dict of
+    radiance-cache options), every job without participating media renders
+    with an online radiance cache."""
     jm = importlib.import_module("hala-pathtracer_gb300.jobmix")
     serve = importlib.import_module("hala-pathtracer_gb300.serve")
     jobs = jm.job_mix(n_jobs=n_jobs, rate=rate, seed=seed)
@@ -434,7 +436,7 @@ def serving_leg(n_jobs=256, rate=20.0, seed=0):
         for j in warm:
             srv.wait(srv.submit(j.scene, j.frames))
         base = srv.stats()
-        res = jm.play(srv, jobs)
+        res = jm.play(srv, jobs, cache=cache)
         st = srv.stats()
     res.update({
         "arrival_rate_jobs_per_s": rate,
@@ -664,6 +666,13 @@ def main():
             line["serving"] = serving_leg(n_jobs=args.serving_jobs)
         except Exception as e:
             line["serving"] = {"error": f"{type(e).__name__}: {e}"}
+        if not args.no_cache:
+            try:
+                sv = serving_leg(n_jobs=args.serving_jobs, cache={})
+                sv["cache"] = "jobs without media rendered with the online radiance cache (default options)"
+                line["serving_with_cache"] = sv
+            except Exception as e:
+                line["serving_with_cache"] = {"error": f"{type(e).__name__}: {e}"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:

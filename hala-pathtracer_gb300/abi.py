@@ -115,7 +115,8 @@ class CacheConfig(C.Structure):
     _fields_ = [("query_depth", C.c_uint32), ("train_shift", C.c_uint32), ("batch_size", C.c_uint32),
                 ("log2_table_size", C.c_uint32), ("learning_rate", C.c_float),
                 ("min_resolution", C.c_uint32), ("max_resolution", C.c_uint32), ("seed", C.c_uint32),
-                ("warmup_frames", C.c_uint32), ("paths_per_pass", C.c_uint32), ("steps_per_pass", C.c_uint32)]
+                ("warmup_frames", C.c_uint32), ("paths_per_pass", C.c_uint32), ("steps_per_pass", C.c_uint32),
+                ("weight_grad_kernel", C.c_uint32)]
 
 
 class ServerConfig(C.Structure):
@@ -130,7 +131,8 @@ class JobDesc(C.Structure):
                 ("env_rgb", C.POINTER(C.c_float)), ("env_width", C.c_uint32),
                 ("env_height", C.c_uint32), ("env_rotation_deg", C.c_float),
                 ("ground_color", C.c_float * 4), ("sky_color", C.c_float * 4),
-                ("env_intensity", C.c_float), ("exposure_value", C.c_float)]
+                ("env_intensity", C.c_float), ("exposure_value", C.c_float),
+                ("cache", C.c_void_p)]
 
 
 class JobInfo(C.Structure):

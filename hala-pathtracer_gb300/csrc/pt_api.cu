@@ -1031,6 +1031,7 @@ pt_status pt_renderer_set_radiance_cache(pt_renderer* r, const pt_cache_config* 
   if (cfg->max_resolution) c.max_resolution = cfg->max_resolution;
   if (cfg->paths_per_pass) c.paths_per_pass = cfg->paths_per_pass;
   c.steps_per_pass = cfg->steps_per_pass;
+  c.weight_grad_kernel = cfg->weight_grad_kernel;
   c.seed = cfg->seed;
   if (c.query_depth == 0) return fail(r, PT_ERR_INVALID_ARG, "query_depth must be at least 1");
   if (c.train_shift > 16) return fail(r, PT_ERR_INVALID_ARG, "train_shift must be at most 16");

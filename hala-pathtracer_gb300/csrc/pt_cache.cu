@@ -635,6 +635,7 @@ __global__ void k_cache_bench_records(float4* rec, float4* tgt, uint32_t n, uint
 constexpr size_t SMEM_INFER = (size_t)(SMEM_WN + INFER_WARPS * TILE) * 2;
 constexpr size_t SMEM_TRAIN = (size_t)(SMEM_WN + SMEM_WK + CACHE_WARPS * TILE) * 2;
 constexpr uint32_t DW_ROWS_PER_BLOCK = 512;
+constexpr uint32_t DW_TC_ROWS_PER_BLOCK = 1024;  // 16 chunks of 64 rows per tensor-core CTA
 
 }  // namespace
 
@@ -668,6 +669,8 @@ struct pt_cache {
   size_t cap = 0;
   Buf<float> partials, loss, gradbuf;
   Buf<float4> rec, tgt;
+  Buf<uint32_t> tc_err;            // wait-limit flag of the tensor-core kernel
+  uint32_t* tc_err_host = nullptr;  // pinned copy, refreshed after every training pass
   uint32_t step = 0;
   float last_loss = 0.0f;
   cudaStream_t stream = nullptr;
@@ -708,10 +711,16 @@ static cudaError_t forward_backward(pt_cache* c, const float4* rec, const float4
   uint32_t blocks = std::min<uint32_t>((tiles + CACHE_WARPS - 1) / CACHE_WARPS, (uint32_t)device_sm_count() * 2);
   k_cache_train_fb<<<blocks, CACHE_WARPS * 32, SMEM_TRAIN, st>>>(c->V, rec, tgt, n, 1.0f / (float)n, c->X.p, c->D.p,
                                                                  c->cap, c->loss.p);
-  const uint32_t nb = (n + DW_ROWS_PER_BLOCK - 1) / DW_ROWS_PER_BLOCK;
-  k_cache_dw<<<dim3(nb, NC_LAYERS), CACHE_WARPS * 32, 0, st>>>(c->X.p, c->D.p, c->cap, n, DW_ROWS_PER_BLOCK,
-                                                               c->partials.p, nb);
-  *nblocks_out = nb;
+  if (c->cfg.weight_grad_kernel == 0) {
+    const uint32_t nb = (n + DW_TC_ROWS_PER_BLOCK - 1) / DW_TC_ROWS_PER_BLOCK;
+    launch_cache_dw_tc(c->X.p, c->D.p, c->cap, n, DW_TC_ROWS_PER_BLOCK, c->partials.p, nb, c->tc_err.p, st);
+    *nblocks_out = nb;
+  } else {
+    const uint32_t nb = (n + DW_ROWS_PER_BLOCK - 1) / DW_ROWS_PER_BLOCK;
+    k_cache_dw<<<dim3(nb, NC_LAYERS), CACHE_WARPS * 32, 0, st>>>(c->X.p, c->D.p, c->cap, n, DW_ROWS_PER_BLOCK,
+                                                                 c->partials.p, nb);
+    *nblocks_out = nb;
+  }
   return cudaGetLastError();
 }
 
@@ -741,8 +750,15 @@ static cudaError_t train_step(pt_cache* c, const float4* rec, const float4* tgt,
   return cudaGetLastError();
 }
 
+// The tensor-core kernel's wait-limit flag as of the last completed pass
+// (the pinned copy is refreshed at the end of every pass, in stream order).
+static cudaError_t tc_status(const pt_cache* c) {
+  return (c->tc_err_host && *c->tc_err_host) ? cudaErrorLaunchTimeout : cudaSuccess;
+}
+
 cudaError_t cache_train_device(pt_cache* c, const float4* rec, const float4* tgt, uint32_t n, cudaStream_t st,
                                uint32_t* steps_done) {
+  if (tc_status(c) != cudaSuccess) return cudaErrorLaunchTimeout;
   uint32_t steps = 0;
   if (n > 0) {
     const uint32_t B = c->cfg.batch_size;
@@ -755,6 +771,8 @@ cudaError_t cache_train_device(pt_cache* c, const float4* rec, const float4* tgt
       if (e != cudaSuccess) return e;
       ++steps;
     }
+    cudaError_t e = cudaMemcpyAsync(c->tc_err_host, c->tc_err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) return e;
   }
   if (steps_done) *steps_done = steps;
   return cudaSuccess;
@@ -783,6 +801,7 @@ void pt_cache_config_default(pt_cache_config* c) {
   std::memset(c, 0, sizeof(*c));
   c->query_depth = 1;
   c->train_shift = 4;
+  c->weight_grad_kernel = 0;
   c->batch_size = 1u << 16;
   c->log2_table_size = 19;
   c->learning_rate = 1e-2f;
@@ -811,7 +830,7 @@ pt_status pt_cache_create(const pt_cache_config* cfg, pt_cache** out) {
   }
   if (c.log2_table_size < 8 || c.log2_table_size > 24 || c.min_resolution < 2 ||
       c.max_resolution < c.min_resolution || c.max_resolution > (1u << 20) || c.batch_size > (1u << 24) ||
-      c.batch_size % 16 != 0 || c.train_shift > 16)
+      c.batch_size % 16 != 0 || c.train_shift > 16 || c.weight_grad_kernel > 1)
     return PT_ERR_INVALID_ARG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PT_ERR_CUDA;
@@ -845,6 +864,9 @@ pt_status pt_cache_create(const pt_cache_config* cfg, pt_cache** out) {
   chk(k->ggrad.ensure(k->grid_count));
   chk(k->gh.ensure(k->grid_count));
   chk(k->loss.ensure(1));
+  chk(k->tc_err.ensure(1));
+  chk(cudaMallocHost(&k->tc_err_host, sizeof(uint32_t)));
+  if (k->tc_err_host) *k->tc_err_host = 0;
   if (e != cudaSuccess) {
     pt_cache_destroy(k);
     return e == cudaErrorMemoryAllocation ? PT_ERR_OOM : PT_ERR_CUDA;
@@ -864,6 +886,7 @@ pt_status pt_cache_create(const pt_cache_config* cfg, pt_cache** out) {
   chk(cudaMemsetAsync(k->gm.p, 0, k->grid_count * sizeof(float), st));
   chk(cudaMemsetAsync(k->gv.p, 0, k->grid_count * sizeof(float), st));
   chk(cudaMemsetAsync(k->ggrad.p, 0, k->grid_count * sizeof(float), st));
+  chk(cudaMemsetAsync(k->tc_err.p, 0, sizeof(uint32_t), st));
   k_cache_set_weights<<<(NC_PARAMS + 255) / 256, 256, 0, st>>>(k->w.p, k->wn.p, k->wk.p);
   const unsigned gb = (unsigned)((k->grid_count + 255) / 256);
   k_cache_init_grid<<<gb, 256, 0, st>>>(k->gw.p, k->grid_count, (uint64_t)c.seed * 7919u + 17u, 1e-4f);
@@ -885,6 +908,7 @@ pt_status pt_cache_create(const pt_cache_config* cfg, pt_cache** out) {
 void pt_cache_destroy(pt_cache* c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->tc_err_host) cudaFreeHost(c->tc_err_host);
   cudaStream_t s = c->stream;
   delete c;
   if (s) cudaStreamDestroy(s);
@@ -989,7 +1013,9 @@ pt_status pt_cache_gradients(pt_cache* c, const float* records, const float* tar
     CCK(c, cudaMemcpyAsync(grid_grad, c->ggrad.p, c->grid_count * sizeof(float), cudaMemcpyDeviceToHost, st));
   if (loss) CCK(c, cudaMemcpyAsync(loss, c->loss.p, sizeof(float), cudaMemcpyDeviceToHost, st));
   CCK(c, cudaMemsetAsync(c->ggrad.p, 0, c->grid_count * sizeof(float), st));
+  CCK(c, cudaMemcpyAsync(c->tc_err_host, c->tc_err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   CCK(c, cudaStreamSynchronize(st));
+  CCK(c, tc_status(c));
   return PT_OK;
 }
 
@@ -1036,6 +1062,7 @@ pt_status pt_cache_benchmark(pt_cache* c, uint32_t n, uint32_t iterations, doubl
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   CCK(c, cudaGetLastError());
+  CCK(c, tc_status(c));
   return PT_OK;
 }
 
@@ -1059,6 +1086,7 @@ pt_status pt_cache_train(pt_cache* c, const float* records, const float* targets
   c->cfg.steps_per_pass = keep;
   if (last_loss) CCK(c, cudaMemcpyAsync(last_loss, c->loss.p, sizeof(float), cudaMemcpyDeviceToHost, st));
   CCK(c, cudaStreamSynchronize(st));
+  CCK(c, tc_status(c));
   return PT_OK;
 }
 

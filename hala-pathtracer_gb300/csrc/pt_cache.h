@@ -50,6 +50,12 @@ namespace hpt {
 cudaError_t cache_train_device(pt_cache* c, const float4* rec, const float4* tgt, uint32_t n, cudaStream_t st,
                                uint32_t* steps_done);
 CacheView cache_view(const pt_cache* c);
+// pt_cache_tc.cu: dW of every layer on the tensor cores (tcgen05, TMEM
+// accumulators) into per-block partials [layer][block][k][n]; *err gets bit 0
+// if a wait for the tensor cores ran out of its iteration limit.
+size_t cache_dw_tc_smem();
+void launch_cache_dw_tc(const __nv_bfloat16* X, const __nv_bfloat16* D, size_t cap, uint32_t n,
+                        uint32_t rows_per_block, float* partials, uint32_t nblocks, uint32_t* err, cudaStream_t st);
 // Loss of the last training batch (synchronous read).
 cudaError_t cache_last_loss(pt_cache* c, float* loss);
 }  // namespace hpt

@@ -56,6 +56,8 @@ struct JobInput {
   uint32_t env_w = 0, env_h = 0;
   float env_rot = 0.0f, env_intensity = 1.0f, exposure = 0.0f;
   float ground[4] = {0, 0, 0, 1}, sky[4] = {0, 0, 0, 1};
+  bool use_cache = false;
+  pt_cache_config cache_cfg{};
   pt_scene_desc desc{};
 
   void copy_from(const pt_job_desc& j) {
@@ -91,11 +93,19 @@ struct JobInput {
     exposure = j.exposure_value;
     std::memcpy(ground, j.ground_color, sizeof(ground));
     std::memcpy(sky, j.sky_color, sizeof(sky));
+    use_cache = j.cache != nullptr;
+    if (use_cache) cache_cfg = *j.cache;
     desc = pt_scene_desc{prims.data(), (uint32_t)prims.size(), mats.data(), (uint32_t)mats.size(),
                          lights.data(), (uint32_t)lights.size(), cams.data(), (uint32_t)cams.size(),
                          texs.data(), (uint32_t)texs.size()};
   }
 };
+
+// Job class bit of a job with a radiance cache: such a job never shares a
+// wavefront (its passes train its own cache in between); the scheduler
+// gives it whole passes through its own renderer, in turn with the shared
+// wavefronts of the other jobs.
+constexpr uint32_t JOB_CACHE_CLASS = 0x100u;
 
 enum : int { ST_QUEUED = PT_JOB_QUEUED, ST_RUNNING = PT_JOB_RUNNING, ST_DONE = PT_JOB_DONE,
              ST_FAILED = PT_JOB_FAILED, ST_CANCELLED = PT_JOB_CANCELLED };
@@ -114,6 +124,7 @@ struct Job {
   uint32_t features = 0;
   uint64_t est = 0;        // admission estimate, counted in resident bytes while held
   uint64_t image_bytes = 0;
+  uint32_t pass_frames = 0;  // frames per turn of a job with a radiance cache
   double t_submit = 0, t_admit = 0, t_done = 0;
   bool cancel = false, release = false, slot_dirty = false;
   bool terminal() const { return state >= ST_DONE; }
@@ -195,7 +206,8 @@ pt_status admit_job(pt_server* s, Job& j, std::string& why) {
   JobInput& in = *j.in;
   pt_tracer_config c = in.cfg;
   c.keep_samples = 0;
-  c.wave_paths = 1;
+  // shared wavefronts use the server's buffers; a cached job renders its own passes
+  c.wave_paths = in.use_cache ? std::max<uint32_t>(in.cache_cfg.paths_per_pass, 1u << 16) : 1;
   pt_renderer* r = nullptr;
   // uploads and BVH builds of admitted jobs go ahead of the running wavefronts
   int least = 0, greatest = 0;
@@ -220,8 +232,14 @@ pt_status admit_job(pt_server* s, Job& j, std::string& why) {
   if ((ps = pt_renderer_set_camera_index(r, in.camera_index)) != PT_OK) return bail(ps);
   if ((ps = pt_renderer_commit(r)) != PT_OK) return bail(ps);
   renderer_drop_build_inputs(r);
-  j.r = r;
   j.features = r->features;
+  if (in.use_cache) {
+    if ((ps = pt_renderer_set_radiance_cache(r, &in.cache_cfg)) != PT_OK) return bail(ps);
+    j.features |= JOB_CACHE_CLASS;
+    const uint64_t per = std::max<uint32_t>(in.cache_cfg.paths_per_pass, 1u);
+    j.pass_frames = (uint32_t)std::max<uint64_t>(1, (per + j.WH - 1) / j.WH);
+  }
+  j.r = r;
   return PT_OK;
 }
 
@@ -301,11 +319,17 @@ bool plan_wave(pt_server* s, std::vector<Segment>& segs, uint32_t cap) {
   if (first == SIZE_MAX) return false;
   s->rr_class = (uint32_t)((first + 1) % n);
   const uint32_t cls = s->running[first]->features;
+  if (cls & JOB_CACHE_CLASS) {  // a pass of its own
+    const JobPtr& j = s->running[first];
+    const uint64_t frames = std::min<uint64_t>(j->pass_frames, (j->total - j->done) / j->WH);
+    segs.push_back(Segment{j, 0, (uint32_t)(frames * j->WH), j->done});
+    return true;
+  }
   std::vector<size_t> members;
   for (size_t k = 0; k < n; ++k) {
     size_t i = (first + k) % n;
     const JobPtr& j = s->running[i];
-    if (!j->cancel && j->done < j->total && j->features == cls) members.push_back(i);
+    if (!j->cancel && j->done < j->total && j->features == cls && !(cls & JOB_CACHE_CLASS)) members.push_back(i);
   }
   std::vector<uint64_t> take(members.size(), 0);
   const uint64_t q = std::max<uint32_t>(s->cfg.quantum_paths, 1);
@@ -439,6 +463,46 @@ void render_loop(pt_server* s) {
     }
     uint32_t total = 0;
     for (const Segment& g : segs) total += g.count;
+    if (segs[0].job->features & JOB_CACHE_CLASS) {
+      JobPtr j = segs[0].job;
+      const uint32_t frames = segs[0].count / j->WH;
+      lk.unlock();
+      const pt_status ps = pt_renderer_render(j->r, frames);
+      const pt_stats rs = j->r->stats;
+      const std::string why = ps == PT_OK ? std::string() : std::string(pt_renderer_last_error(j->r));
+      lk.lock();
+      ++s->st.wavefronts;
+      if (ps != PT_OK) {
+        auto it = std::find(s->running.begin(), s->running.end(), j);
+        if (it != s->running.end()) s->running.erase(it);
+        s->resident -= j->est;
+        finish_job(s, j, ST_FAILED, ps, why);
+        dead.push_back(j);
+        continue;
+      }
+      s->st.paths += rs.paths;
+      s->st.closest_rays += rs.closest_rays;
+      s->st.shadow_rays += rs.shadow_rays;
+      s->st.busy_ms += rs.render_ms;
+      s->st.kernel_launches += rs.kernel_launches;
+      j->done += (uint64_t)frames * j->WH;
+      if (j->done == j->total) {
+        auto it = std::find(s->running.begin(), s->running.end(), j);
+        if (it != s->running.end()) s->running.erase(it);
+        s->resident -= j->est - j->image_bytes;
+        j->est = j->image_bytes;
+        finish_job(s, j, ST_DONE, PT_OK, "");
+        lk.unlock();
+        {
+          std::lock_guard<std::mutex> g2(j->io);
+          pt_renderer_set_radiance_cache(j->r, nullptr);
+          j->r->W.release();
+          renderer_drop_scene(j->r);
+        }
+        lk.lock();
+      }
+      continue;
+    }
     lk.unlock();
     uint64_t bounce_launches = 0;
     bool timed_out = false;
@@ -585,10 +649,28 @@ pt_status pt_server_submit(pt_server* s, const pt_job_desc* jd, uint64_t* job_id
   if (v == PT_OK && jd->camera_index >= jd->scene->num_cameras) v = PT_ERR_INVALID_ARG, why = "camera index out of range";
   if (v == PT_OK && jd->env_rgb && (jd->env_width == 0 || jd->env_height == 0))
     v = PT_ERR_INVALID_ARG, why = "environment map without a size";
+  if (v == PT_OK && jd->cache) {
+    for (uint32_t i = 0; i < jd->scene->num_materials; ++i)
+      if (jd->scene->materials[i].medium.type != PT_MEDIUM_NONE) {
+        v = PT_ERR_UNSUPPORTED;
+        why = "the radiance cache does not support participating media";
+        break;
+      }
+  }
   const uint32_t ew = jd->env_rgb ? jd->env_width : 0, eh = jd->env_rgb ? jd->env_height : 0;
   uint64_t est = 0;
   if (v == PT_OK) {
     est = renderer_estimate_bytes(jd->scene, jd->config.width, jd->config.height, ew, eh);
+    if (jd->cache) {
+      // the cache (hash table with its Adam state, MLP), its per-path buffers
+      // and the job's own wavefront of paths_per_pass paths
+      const uint32_t log2t = jd->cache->log2_table_size ? jd->cache->log2_table_size : 19;
+      const uint64_t per = std::max<uint32_t>(jd->cache->paths_per_pass ? jd->cache->paths_per_pass : 1u << 20,
+                                              1u << 16);
+      const uint64_t batch = jd->cache->batch_size ? jd->cache->batch_size : 1u << 16;
+      est += 16ull * (1ull << log2t) * 2 * 18 + per * (WaveBuffers::bytes_per_path(false, false) + 240) +
+             batch * 64 * 6 * 2 * 2 + (16u << 20);
+    }
     if (est > s->cfg.hbm_budget_bytes) {
       v = PT_ERR_OOM;
       why = "job needs about " + std::to_string(est >> 20) + " MiB, more than the whole budget of " +

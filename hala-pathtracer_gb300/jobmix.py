@@ -98,12 +98,16 @@ def job_mix(n_jobs=256, rate=20.0, seed=0, bases=None, min_pixels=128 * 128, max
     return jobs
 
 
-def play(server, jobs, time_scale=1.0, release=True):
+def play(server, jobs, time_scale=1.0, release=True, cache=None):
     """Submits each job at its arrival time, waits for all of them and
     returns a summary: job latencies (submit to done, server clock), their
     p50/p99, and paths/s over the span from the first submit to the last
-    completion."""
-    descs = [server.job_desc(j.scene, j.frames) for j in jobs]
+    completion. With `cache` (pt_cache_config fields as a dict), every job
+    whose scene has no participating medium renders with an online radiance
+    cache (the cache does not handle media)."""
+    def wants_cache(j):
+        return cache is not None and all(m.medium.type == abi.MEDIUM_NONE for m in j.scene.materials)
+    descs = [server.job_desc(j.scene, j.frames, cache if wants_cache(j) else None) for j in jobs]
     t0 = time.perf_counter()
     done = threading.Event()
     waiter_err = []

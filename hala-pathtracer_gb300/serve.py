@@ -14,7 +14,7 @@ import ctypes as C
 import numpy as np
 
 from . import abi
-from . import PTError, _f4, load_library
+from . import PTError, _cache_config, _f4, load_library
 
 
 class Server:
@@ -57,9 +57,11 @@ class Server:
             msg = self._lib.pt_server_last_error(self._h)
             raise PTError(st, msg.decode() if msg else "")
 
-    def job_desc(self, scene, frames=None, **cfg_over):
+    def job_desc(self, scene, frames=None, cache=None, **cfg_over):
         """pt_job_desc for a scenes.Scene, set up the way `renderer_for` sets
-        up a renderer. Returns (desc, keepalive)."""
+        up a renderer; `cache` (a dict of pt_cache_config fields, {} for the
+        defaults) renders the job with an online radiance cache. Returns
+        (desc, keepalive)."""
         desc = scene.desc()
         jd = abi.JobDesc()
         jd.scene = C.pointer(desc)
@@ -67,6 +69,10 @@ class Server:
         jd.frames = int(scene.spp if frames is None else frames)
         jd.camera_index = 0
         keep = [scene, desc]
+        if cache is not None:
+            cc = _cache_config(**cache)
+            keep.append(cc)
+            jd.cache = C.addressof(cc)
         if scene.env_rgb is not None:
             env = np.ascontiguousarray(scene.env_rgb, np.float32)
             keep.append(env)
@@ -82,9 +88,9 @@ class Server:
         jd.exposure_value = float(scene.exposure_value)
         return jd, keep
 
-    def submit(self, scene, frames=None, **cfg_over):
+    def submit(self, scene, frames=None, cache=None, **cfg_over):
         """Queues one job; returns its id. The scene's arrays are copied."""
-        jd, keep = self.job_desc(scene, frames, **cfg_over)
+        jd, keep = self.job_desc(scene, frames, cache, **cfg_over)
         return self.submit_desc(jd)
 
     def submit_desc(self, job_desc):

@@ -403,6 +403,7 @@ pt_status pt_bvh_build_noalloc(const void* tri_v0, const void* tri_e1, const voi
  *
  * Thread safety: every pt_server_* call may come from any host thread. */
 typedef struct pt_server pt_server;
+typedef struct pt_cache_config pt_cache_config;
 
 typedef struct pt_server_config {
   uint64_t hbm_budget_bytes; /* device bytes for admitted jobs; 0 = 80% of free memory at create */
@@ -429,6 +430,9 @@ typedef struct pt_job_desc {
   float sky_color[4];           /* set_sky_color */
   float env_intensity;          /* set_env_intensity */
   float exposure_value;         /* set_exposure_value */
+  const pt_cache_config* cache; /* non-NULL: render with an online radiance cache of this
+                                   configuration (pt_renderer_set_radiance_cache); such a job
+                                   runs its passes on its own, between shared wavefronts */
 } pt_job_desc;
 
 typedef enum pt_job_state {
@@ -515,7 +519,7 @@ pt_status pt_server_get_stats(pt_server* s, pt_server_stats* out);
  * metallic, specular transmission, 0. */
 typedef struct pt_cache pt_cache;
 
-typedef struct pt_cache_config {
+struct pt_cache_config {
   uint32_t query_depth;     /* vertex index at which paths end in the cache (1 = first bounce) */
   uint32_t train_shift;     /* 1 in 2^train_shift paths trains the cache (4 = 1/16) */
   uint32_t batch_size;      /* training batch in samples (multiple of 16) */
@@ -529,7 +533,10 @@ typedef struct pt_cache_config {
                                between wavefronts, so smaller passes adapt sooner */
   uint32_t steps_per_pass;  /* optimiser steps after each pass at least (batches cycle
                                through the pass's samples) */
-} pt_cache_config;
+  uint32_t weight_grad_kernel; /* weight gradients: 0 = tcgen05 tensor-core kernel with the
+                                  accumulator in tensor memory, 1 = the warp-level mma.sync
+                                  kernel (kept for comparison) */
+};
 
 /* query_depth 1, 1/16 training paths, batch 65536, 2^19 entries, lr 1e-2,
  * resolutions 16..2048, seed 1, one warm-up frame, passes of 2^20 paths,

@@ -119,6 +119,36 @@ def test_gpu_gradients_match_cpu(cache_mod, n):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("n", [64, 1000, 70000])
+def test_tensor_core_weight_gradients_match_the_warp_kernel(cache_mod, n):
+    """The weight gradients of the tcgen05 kernel (TMEM accumulators) equal
+    those of the warp-level mma.sync kernel up to fp32 summation order, for
+    ragged batches (n not a multiple of the 64-row chunk) and batches over
+    several 1024-row blocks."""
+    log2 = 14
+    out = []
+    for kernel in (0, 1):
+        c = cache_mod.RadianceCache(log2_table_size=log2, seed=5, weight_grad_kernel=kernel)
+        c.set_bounds(LO, HI)
+        mlp, grid = random_params(9, log2)
+        c.set_params(mlp, grid)
+        rec, tgt = batch(n, 10)
+        out.append(c.gradients(rec, tgt))
+        c.close()
+    (ga, gga, la), (gb, ggb, lb) = out
+    # loss and table gradient: the same kernel, float atomics in any order
+    assert abs(la - lb) <= 1e-5 * abs(lb)
+    assert np.linalg.norm(gga - ggb) <= 1e-5 * np.linalg.norm(ggb)
+    for l in range(cr.LAYERS):
+        k, m = cr.layer_shape(l)
+        a = ga[cr.layer_off(l):cr.layer_off(l) + k * m]
+        b = gb[cr.layer_off(l):cr.layer_off(l) + k * m]
+        err = np.abs(a - b).max() / max(np.abs(b).max(), 1e-30)
+        assert err < 1e-4, (l, err)
+        assert np.count_nonzero(b) == 0 or np.count_nonzero(a) > 0
+
+
+@pytest.mark.gpu
 def test_gpu_training_fits_a_smooth_field(cache_mod):
     c = cache_mod.RadianceCache(log2_table_size=16, seed=11, batch_size=4096)
     c.set_bounds(LO, HI)

@@ -187,3 +187,58 @@ def test_job_mix_is_seeded_and_within_bounds(jobmix):
         base = bases[j.kind]
         assert j.scene.meshes is base.meshes
         assert len(j.scene.materials) == len(base.materials)
+
+
+@pytest.mark.gpu
+def test_radiance_cache_jobs_alone_and_in_the_mix(pt, serve, scenes):
+    """Jobs with an online radiance cache run their passes on their own,
+    between the shared wavefronts of plain jobs. The cache's hash-table
+    gradients are summed with float atomics, whose order varies from run to
+    run, so a cached render is reproducible to within that training noise,
+    not bit for bit: a cached job's accumulated image alone on a server, in a
+    mix with plain and other cached jobs, and through pt_renderer with the
+    same frames per render call agree within 2% relative RMS (the stated
+    tolerance). Plain jobs in the mix stay bit-identical. A cached job on a
+    scene with media is refused at submit."""
+    cache = dict(paths_per_pass=1 << 14, batch_size=4096, log2_table_size=14, steps_per_pass=2)
+    a = scenes.cornell(48, 32, 12, max_depth=6, rr_depth=2, seed=3)
+    b = scenes.cornell(40, 40, 9, max_depth=5, rr_depth=2, seed=4)
+    plain = pin_scenes.disney_ibl()
+    with serve.Server(wave_paths=1 << 14, quantum_paths=1 << 12) as srv:
+        ja = srv.submit(a, cache=cache)
+        assert srv.wait(ja, 120000)
+        alone_a = [srv.image(ja, k) for k in IMAGES]
+    with serve.Server(wave_paths=1 << 14, quantum_paths=1 << 12) as srv:
+        srv.pause(True)
+        ids = [srv.submit(plain), srv.submit(a, cache=cache), srv.submit(b, cache=cache), srv.submit(plain)]
+        srv.pause(False)
+        for jid in ids:
+            assert srv.wait(jid, 120000)
+            assert srv.poll(jid).state == pt.abi.JOB_DONE, srv.poll(jid).error
+        mixed_a = [srv.image(ids[1], k) for k in IMAGES]
+        plain_imgs = [srv.image(ids[0], k) for k in IMAGES]
+        st = srv.stats()
+        assert st.paths == 2 * plain.width * plain.height * plain.spp + a.width * a.height * 12 + \
+            b.width * b.height * 9
+        with pytest.raises(pt.PTError) as e:
+            srv.submit(scenes.media_box(16, 16, 1), cache=cache)
+        assert e.value.status == pt.abi.PT_ERR_UNSUPPORTED
+    def rel_rms(x, y):
+        x, y = x[..., :3].astype(np.float64), y[..., :3].astype(np.float64)
+        return float(np.sqrt(((x - y) ** 2).mean() / max((y ** 2).mean(), 1e-30)))
+    assert rel_rms(mixed_a[0], alone_a[0]) < 2e-2
+    assert rel_rms(mixed_a[1], alone_a[1]) < 1e-6 and rel_rms(mixed_a[2], alone_a[2]) < 1e-6  # first-hit AOVs
+    ref = alone(pt, plain, plain.spp)
+    for k in IMAGES:
+        assert np.array_equal(plain_imgs[k].view(np.uint8), ref[k].view(np.uint8)), k
+    # the server's turns are render calls of whole passes: 16384 paths = 10.67
+    # frames of 48 x 32, so turns of 11 frames, then the last frame
+    r = pt.renderer_for(a, wave_paths=1 << 14)
+    r.set_radiance_cache(**cache)
+    r.render(11)
+    r.render(1)
+    assert rel_rms(r.image(0), alone_a[0]) < 2e-2
+    assert r.stats().frame_index == 12
+    # and the cache did take part: the cached render is not the plain one
+    plain_a = alone(pt, a, 12)
+    assert rel_rms(alone_a[0], plain_a[0]) > 1e-4
