@@ -261,24 +261,36 @@ def progressive_frames(r, abi, frames):
     return out
 
 
-def l2_copy_bandwidth(torch, mib=32, reps=50):
+def l2_copy_bandwidth(torch, mib=32, reps=64):
     """GB/s (read + write) of a device copy between two buffers that stay in
     the 129 MB L2: the ceiling for L2-served traffic the roofline's L2
-    fraction is quoted against."""
+    fraction is quoted against. The copies are replayed from a CUDA graph so
+    that launch gaps do not count; best of five replays."""
     n = (mib << 20) // 4
     a = torch.ones(n, dtype=torch.float32, device="cuda")
     b = torch.empty_like(a)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        for _ in range(3):
+            b.copy_(a)
+    torch.cuda.current_stream().wait_stream(s)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        for _ in range(reps):
+            b.copy_(a)
+    g.replay()
+    best = None
     for _ in range(5):
-        b.copy_(a)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record()
-    for _ in range(reps):
-        b.copy_(a)
-    e1.record()
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    return 2.0 * (mib << 20) * reps / (ms / 1e3) / 1e9
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        g.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    return 2.0 * (mib << 20) * reps / (best / 1e3) / 1e9
 
 
 def workloads_leg(pt):
@@ -623,7 +635,8 @@ def main():
                      "traffic_note": "ncu DRAM bytes per ray (480x270 capture, bounces 0-1) x rays per launch",
                      "dram_achieved_gbs": dram_gbs, "dram_frac": dram_gbs / peak,
                      "l2": {"achieved": achieved, "peak": l2_gbs, "frac": achieved / l2_gbs if l2_gbs else None,
-                            "peak_kind": "measured here: torch copy between two 32 MiB buffers resident in L2"},
+                            "peak_kind": "measured here: copies between two 32 MiB buffers resident in L2, replayed "
+                                         "from a CUDA graph"},
                      "limiter": "issue and dependent-load latency: the BVH and triangles stay in L2 (72-81% L2 "
                                 "hit rate), DRAM carries ~67 B per ray; ncu shows 64-66% issue active and 8-11 "
                                 "of 32 lanes active per instruction (divergent traversal lengths)",

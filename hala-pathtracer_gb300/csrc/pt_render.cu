@@ -112,40 +112,15 @@ __global__ void k_camera_multi(PathState P, const WaveSegment* segs, uint32_t ns
 }
 
 // ------------------------------------------------------------------ trace
-// Each block takes 256 consecutive queue entries (neighbouring pixels, so
-// nearby origins) and regroups them by the octant of the ray direction before
-// tracing (a counting sort in shared memory): a warp then holds rays whose
-// slab tests pick the same near planes and whose nearest-first child orders
-// agree, so its lanes walk the BVH more alike. The order in which rays are
-// traced does not change any result.
 constexpr uint32_t TRACE_BLOCK = 256;
 
 template <bool BRUTE, bool COUNT, bool MULTI>
 __global__ void __launch_bounds__(TRACE_BLOCK, 5) k_trace(const __grid_constant__ DevScene S0, PathState P,
                                                           QueueSet Q) {
-  __shared__ uint32_t s_path[TRACE_BLOCK];
-  __shared__ uint32_t s_count[9];  // eight octants + the empty slots of a partial block
   const uint32_t n = *Q.in_count;
   TravCount tc;
-  for (uint32_t base = blockIdx.x * TRACE_BLOCK; base < n; base += gridDim.x * TRACE_BLOCK) {
-    const uint32_t i = base + threadIdx.x;
-    uint32_t p = 0xFFFFFFFFu, key = 8u;
-    if (i < n) {
-      p = Q.in[i];
-      const float4 d4 = P.ray_d[p];
-      key = (d4.x < 0.0f ? 1u : 0u) | (d4.y < 0.0f ? 2u : 0u) | (d4.z < 0.0f ? 4u : 0u);
-    }
-    if (threadIdx.x < 9) s_count[threadIdx.x] = 0u;
-    __syncthreads();
-    const uint32_t rank = atomicAdd(&s_count[key], 1u);
-    __syncthreads();
-    uint32_t off = 0;
-    for (uint32_t k = 0; k < key; ++k) off += s_count[k];
-    s_path[off + rank] = p;
-    __syncthreads();
-    p = s_path[threadIdx.x];
-    __syncthreads();  // s_count and s_path are rewritten by the next round
-    if (p == 0xFFFFFFFFu) continue;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    uint32_t p = Q.in[i];
     const DevScene& S = MULTI ? P.jobs[P.job[p]] : S0;
     if (P.c_train) {
       // a training path leaving the cache vertex: what it gathered so far is

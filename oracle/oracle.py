@@ -65,6 +65,9 @@ def lib():
             "or_read_image": (C.c_int, [P, C.c_int, C.c_void_p, C.c_size_t]),
             "or_trace_paths": (C.c_int, [P, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32), C.c_uint32,
                                          C.POINTER(C.c_float), C.POINTER(C.c_uint32), C.c_int]),
+            "or_set_brute": (None, [P, C.c_int]),
+            "or_trace_path_rays": (C.c_int, [P, C.c_uint32, C.c_uint32, C.POINTER(C.c_float), C.c_uint32,
+                                             C.POINTER(C.c_uint32)]),
             "or_trace_rays": (C.c_int, [P, C.POINTER(C.c_float), C.c_uint32, C.c_int, C.c_int,
                                         C.POINTER(C.c_uint32), C.c_int]),
             "or_counters": (None, [P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
@@ -178,6 +181,22 @@ class Oracle:
         if rc != 0:
             raise RuntimeError(f"trace_paths failed {rc}")
         return rad, hsh
+
+    def path_rays(self, pixel, frame):
+        """The rays one path traces, in order: (n, 11) float32 rows of origin,
+        tmin, direction, tmax, kind (0 closest hit, 1 any hit), result bits
+        (hit id or occluded), t."""
+        cap = 4096
+        out = np.zeros((cap, 11), np.float32)
+        n = C.c_uint32()
+        rc = lib().or_trace_path_rays(self.h, int(pixel), int(frame), _fp(out), cap, C.byref(n))
+        if rc != 0:
+            raise RuntimeError(f"trace_path_rays failed {rc}")
+        return out[:min(n.value, cap)]
+
+    def set_brute_force(self, on=True):
+        """Trace paths against every triangle instead of the BVH."""
+        lib().or_set_brute(self.h, 1 if on else 0)
 
     def trace_rays(self, rays, any_hit=False, brute_force=False, threads=0):
         rays = np.ascontiguousarray(rays, np.float32)

@@ -333,6 +333,7 @@ struct BNode {
 
 struct Ctx {
   pt_tracer_config cfg{};
+  bool force_brute = false;  // paths traced against every triangle instead of the BVH (checks)
   // flattened geometry
   std::vector<V3> tv0, te1, te2;            // per triangle, world space
   std::vector<uint32_t> tidx;               // 3 global vertex indices per triangle
@@ -405,7 +406,7 @@ inline bool slab(const AABB& b, const V3& o, const V3& inv, float tmin, float tm
                           std::fmax(std::fmin(tz0, tz1), tmin));
   float tfar = std::fmin(std::fmin(std::fmax(tx0, tx1), std::fmax(ty0, ty1)),
                          std::fmin(std::fmax(tz0, tz1), tmax));
-  tfar *= 1.00000024f;
+  tfar *= 1.0000005f;
   tn = tnear;
   return tnear <= tfar;
 }
@@ -1350,12 +1351,24 @@ struct Tracer {
   Ray ray;
   uint32_t hash = HASH_INIT;
   uint32_t n_closest = 0, n_shadow = 0;
+  // optional record of every ray the path traces (or_trace_path_rays):
+  // origin xyz, tmin, direction xyz, tmax, kind (0 closest, 1 any-hit), hit id / occluded, t
+  std::vector<float>* rec = nullptr;
 
   explicit Tracer(const Ctx& cc) : c(cc) {}
 
+  void record(const Ray& r, float tmax, uint32_t kind, uint32_t result, float t) {
+    if (!rec) return;
+    const float v[11] = {r.o.x, r.o.y, r.o.z, 0.0f, r.d.x, r.d.y, r.d.z, tmax, (float)kind, 0.0f, t};
+    rec->insert(rec->end(), v, v + 11);
+    std::memcpy(&(*rec)[rec->size() - 2], &result, 4);
+  }
+
   Hit closest(const Ray& r) {
     ++n_closest;
-    return trace_closest(c, r, 0.0f, WORLD_SIZE, false);
+    Hit h = trace_closest(c, r, 0.0f, WORLD_SIZE, c.force_brute);
+    record(r, WORLD_SIZE, 0, h.id, h.t);
+    return h;
   }
 
   // inc/lighting.glsl:7-61 (MEDIUM && VOL_MIS); draws from the main path RNG.
@@ -1368,7 +1381,8 @@ struct Tracer {
     V3 T(1.0f);
     for (int depth = 0; depth < (int)c.cfg.max_depth; ++depth) {
       ++n_shadow;
-      Hit h = trace_closest(c, r, 0.0f, WORLD_SIZE, false);
+      Hit h = trace_closest(c, r, 0.0f, WORLD_SIZE, c.force_brute);
+      record(r, WORLD_SIZE, 0, h.id, h.t);
       fill_state(c, r, h, ts);
       if ((ts.flags & RAY_FLAGS_HIT) == 0 || (ts.flags & RAY_FLAGS_IS_EMITTER) != 0) break;
       if (ts.material_index >= c.mats.size()) return V3(0.0f);
@@ -1388,7 +1402,9 @@ struct Tracer {
 
   bool occluded(const Ray& r, float tmax) {
     ++n_shadow;
-    return trace_any(c, r, 0.0f, tmax, false);
+    const bool occ = trace_any(c, r, 0.0f, tmax, c.force_brute);
+    record(r, tmax, 1, occ ? 1u : 0u, 0.0f);
+    return occ;
   }
 
   // inc/lighting.glsl:69-244
@@ -2021,6 +2037,27 @@ int or_trace_paths(or_ctx* o, uint32_t first_frame, uint32_t nframes, const uint
     c.n_shadow += ns;
   });
   return PT_OK;
+}
+
+// Every ray of one path (pixel, frame), 11 floats each (see Tracer::record);
+// *count receives the number of rays, at most `cap` are written.
+int or_trace_path_rays(or_ctx* o, uint32_t pixel, uint32_t frame, float* out, uint32_t cap, uint32_t* count) {
+  if (!o || !out || !count) return PT_ERR_INVALID_ARG;
+  Ctx& c = o->c;
+  if (!c.committed) return PT_ERR_STATE;
+  std::vector<float> rec;
+  Tracer tr(c);
+  tr.rec = &rec;
+  tr.run(pixel % c.cfg.width, pixel / c.cfg.width, frame);
+  const uint32_t n = (uint32_t)(rec.size() / 11);
+  *count = n;
+  std::memcpy(out, rec.data(), sizeof(float) * 11 * std::min(n, cap));
+  return PT_OK;
+}
+
+// Paths traced against every triangle (1) or through the BVH (0, default).
+void or_set_brute(or_ctx* o, int brute) {
+  if (o) o->c.force_brute = brute != 0;
 }
 
 int or_trace_rays(or_ctx* o, const float* rays, uint32_t n, int any_hit, int brute, uint32_t* hits,

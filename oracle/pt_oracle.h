@@ -51,6 +51,11 @@ int or_trace_paths(or_ctx* c, uint32_t first_frame, uint32_t nframes, const uint
                    uint32_t npix, float* radiance_out, uint32_t* hash_out, int threads);
 
 /* Geometry queries with the same ray/hit layout as pt_renderer_trace_rays. */
+// Every ray one path traces: origin xyz, tmin, direction xyz, tmax, kind
+// (0 closest, 1 any-hit), result bits (hit id / occluded), t; 11 floats each.
+int or_trace_path_rays(or_ctx* c, uint32_t pixel, uint32_t frame, float* out, uint32_t cap, uint32_t* count);
+// Paths traced against every triangle (1) instead of the BVH (0, the default).
+void or_set_brute(or_ctx* c, int brute);
 int or_trace_rays(or_ctx* c, const float* rays, uint32_t n, int any_hit, int brute_force,
                   uint32_t* hits, int threads);
 
