@@ -810,7 +810,7 @@ void pt_cache_config_default(pt_cache_config* c) {
   c->seed = 1;
   c->warmup_frames = 1;
   c->paths_per_pass = 1u << 20;
-  c->steps_per_pass = 4;
+  c->steps_per_pass = 1;
 }
 
 pt_status pt_cache_create(const pt_cache_config* cfg, pt_cache** out) {

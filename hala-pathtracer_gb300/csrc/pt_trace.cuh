@@ -143,10 +143,21 @@ __device__ __forceinline__ SlabRay slab_ray(float3 o, float3 d) {
   return r;
 }
 
+// Culling slack on the current hit distance (2^-12 relative). A triangle's
+// computed t carries the rounding of the intersection test, which grows as
+// the ray grazes the triangle's plane or the triangle is small against its
+// distance (a shared-edge hit on the 1080p Disney grid was 21 ulps early),
+// while a box's entry distance is close to exact: a box is only culled when
+// it starts beyond best * (1 + 2^-12), so no triangle whose computed t beats
+// the best is skipped. The oracle's BVH uses the same slack.
+constexpr float TRAV_T_SLACK = 1.0f + 1.0f / 4096.0f;
+
 // Slab test of the four children of a 4-wide node, one lane per child. The
 // near and far planes of each axis are picked by the ray's direction signs
 // when loading, which gives exactly min/max of the two plane distances (the
-// distance is monotonic in the plane coordinate, lo <= hi).
+// distance is monotonic in the plane coordinate, lo <= hi). The slab interval
+// gets a few ulps of slack for its own rounding; `tmax` (the best hit so far)
+// gets TRAV_T_SLACK.
 __device__ __forceinline__ void quad_slabs(const float4* nd, const SlabRay& r, float tmin, float tmax,
                                            float (&tn)[4], bool (&hit)[4]) {
   const float4 nx = __ldg(nd + r.nx), fx = __ldg(nd + 1 - r.nx);
@@ -155,15 +166,16 @@ __device__ __forceinline__ void quad_slabs(const float4* nd, const SlabRay& r, f
   const float NX[4] = {nx.x, nx.y, nx.z, nx.w}, FX[4] = {fx.x, fx.y, fx.z, fx.w};
   const float NY[4] = {ny.x, ny.y, ny.z, ny.w}, FY[4] = {fy.x, fy.y, fy.z, fy.w};
   const float NZ[4] = {nz.x, nz.y, nz.z, nz.w}, FZ[4] = {fz.x, fz.y, fz.z, fz.w};
+  const float tcap = tmax * TRAV_T_SLACK;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     float a0 = fmaf(NX[k], r.inv.x, -r.oinv.x), b0 = fmaf(FX[k], r.inv.x, -r.oinv.x);
     float a1 = fmaf(NY[k], r.inv.y, -r.oinv.y), b1 = fmaf(FY[k], r.inv.y, -r.oinv.y);
     float a2 = fmaf(NZ[k], r.inv.z, -r.oinv.z), b2 = fmaf(FZ[k], r.inv.z, -r.oinv.z);
     float n = fmaxf(fmaxf(a0, a1), fmaxf(a2, tmin));
-    float f = fminf(fminf(b0, b1), fminf(b2, tmax));
+    float f = fminf(fminf(b0, b1), b2) * 1.0000005f;
     tn[k] = n;
-    hit[k] = n <= f * 1.0000005f;
+    hit[k] = n <= fminf(f, tcap);
   }
 }
 
@@ -249,7 +261,7 @@ __device__ __forceinline__ HitRec trace_tris_closest(const DevScene& S, float3 o
         cur = 0x7FFFFFFF;
         while (sp > 0) {
           --sp;
-          if (st_t[sp] <= h.t * 1.0000005f) {
+          if (st_t[sp] <= h.t * TRAV_T_SLACK) {
             cur = st_link[sp];
             break;
           }
@@ -277,7 +289,7 @@ __device__ __forceinline__ HitRec trace_tris_closest(const DevScene& S, float3 o
     cur = 0x7FFFFFFF;
     while (sp > 0) {
       --sp;
-      if (st_t[sp] <= h.t * 1.0000005f) {
+      if (st_t[sp] <= h.t * TRAV_T_SLACK) {
         cur = st_link[sp];
         break;
       }

@@ -540,7 +540,7 @@ struct pt_cache_config {
 
 /* query_depth 1, 1/16 training paths, batch 65536, 2^19 entries, lr 1e-2,
  * resolutions 16..2048, seed 1, one warm-up frame, passes of 2^20 paths,
- * at least 4 steps per pass. */
+ * at least one optimiser step per pass, tcgen05 weight gradients. */
 void pt_cache_config_default(pt_cache_config* config);
 pt_status pt_cache_create(const pt_cache_config* config, pt_cache** out);
 void pt_cache_destroy(pt_cache* cache);

@@ -398,15 +398,19 @@ inline bool intersect_tri(const V3& o, const V3& d, const V3& v0, const V3& e1, 
 
 // Slab test; the far distance is widened by 2 ulp-ish so a box never misses
 // a triangle it contains (Ize 2013). Same arithmetic on the device.
+// Conservative slab test: a few ulps of slack on the slab interval, and
+// 2^-12 relative slack on tmax (the best hit so far): a triangle's computed t
+// can be early by many ulps when the ray grazes it or it is small against its
+// distance, and its box must not be culled for that (the device traversal
+// uses the same slack).
 inline bool slab(const AABB& b, const V3& o, const V3& inv, float tmin, float tmax, float& tn) {
   float tx0 = (b.lo.x - o.x) * inv.x, tx1 = (b.hi.x - o.x) * inv.x;
   float ty0 = (b.lo.y - o.y) * inv.y, ty1 = (b.hi.y - o.y) * inv.y;
   float tz0 = (b.lo.z - o.z) * inv.z, tz1 = (b.hi.z - o.z) * inv.z;
   float tnear = std::fmax(std::fmax(std::fmin(tx0, tx1), std::fmin(ty0, ty1)),
                           std::fmax(std::fmin(tz0, tz1), tmin));
-  float tfar = std::fmin(std::fmin(std::fmax(tx0, tx1), std::fmax(ty0, ty1)),
-                         std::fmin(std::fmax(tz0, tz1), tmax));
-  tfar *= 1.0000005f;
+  float tfar = std::fmin(std::fmin(std::fmax(tx0, tx1), std::fmax(ty0, ty1)), std::fmax(tz0, tz1));
+  tfar = std::fmin(tfar * 1.0000005f, tmax * (1.0f + 1.0f / 4096.0f));
   tn = tnear;
   return tnear <= tfar;
 }
