@@ -320,15 +320,25 @@ def workloads_leg(pt):
         row["host_loop_render_ms"] = r.stats().render_ms
         r.set_profiling(0)
         if name.startswith("displaced"):
-            # BVH rebuilt and timed per frame
-            r.reset()
-            total = 0.0
-            for _ in range(s.spp):
+            # BVH rebuilt and timed per frame, with the default (SAH) and the
+            # fast (Morton-ordered linear BVH) builder
+            for key, mode in (("per_frame_rebuild", abi.BVH_BUILD_SAH), ("per_frame_rebuild_fast", abi.BVH_BUILD_FAST)):
+                r.set_bvh_build(mode)
                 r.commit()
-                total += r.stats().bvh_build_ms
-                r.render(1)
-                total += r.stats().render_ms
-            row["per_frame_rebuild"] = {"paths_per_s": st.paths / (total / 1e3), "ms_total": total}
+                r.reset()
+                r.render(1)  # warm-up of this tree
+                r.reset()
+                total, build = 0.0, 0.0
+                for _ in range(s.spp):
+                    r.commit()
+                    build += r.stats().bvh_build_ms
+                    r.render(1)
+                    total += r.stats().render_ms
+                total += build
+                row[key] = {"paths_per_s": st.paths / (total / 1e3), "ms_total": total,
+                            "build_ms_per_frame": build / s.spp, "render_ms_per_frame": (total - build) / s.spp}
+            r.set_bvh_build(abi.BVH_BUILD_SAH)
+            r.commit()
         r.reset()
         r.render(s.spp)  # the render whose pixels the CPU sample checks (the rebuild loop above changed accum)
         acc = r.image(abi.IMAGE_ACCUM)

@@ -189,6 +189,10 @@ class Renderer:
                                                        hsh.ctypes.data))
         return rad, hsh
 
+    def set_bvh_build(self, mode):
+        """abi.BVH_BUILD_SAH (default) or abi.BVH_BUILD_FAST for the next commit()."""
+        self._check(self._lib.pt_renderer_set_bvh_build(self._h, int(mode)))
+
     def set_traversal_limits(self, stack_entries=0, max_visits=0):
         """Traversal stack entries (1..96) and node visits per ray; 0 = default."""
         self._check(self._lib.pt_renderer_set_traversal_limits(self._h, int(stack_entries), int(max_visits)))
@@ -224,10 +228,13 @@ class Renderer:
         return hits
 
 
-def renderer_for(scene, **cfg_over):
+def renderer_for(scene, bvh_build=None, **cfg_over):
     """Creates, fills and commits a renderer for a procedural scene, in the
-    order of src/bin/hala-pathtracer.rs:128-213."""
+    order of src/bin/hala-pathtracer.rs:128-213 (`bvh_build`: the BVH
+    builder, abi.BVH_BUILD_SAH by default)."""
     r = Renderer(scene.config(**cfg_over))
+    if bvh_build is not None:
+        r.set_bvh_build(bvh_build)
     r.set_scene(scene)
     if scene.env_rgb is not None:
         r.set_envmap(scene.env_rgb, scene.env_rotation_deg)

@@ -161,6 +161,7 @@ PROFILE_TRACE_TIMING = 1
 PROFILE_COUNT = 2
 PROFILE_HOST_LOOP = 4
 NOALLOC_MAX_TRIANGLES = 65536
+BVH_BUILD_SAH, BVH_BUILD_FAST = 0, 1
 
 
 def make_config(width, height, max_depth=8, rr_depth=0, enable_tonemap=True, enable_aces=True,
@@ -206,6 +207,7 @@ RENDERER_SIGNATURES = {
     "pt_renderer_set_profiling": (C.c_int, [C.c_void_p, C.c_uint32]),
     "pt_renderer_trace_rays": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_uint32,
                                          C.c_int32, C.c_int32, C.POINTER(C.c_uint32)]),
+    "pt_renderer_set_bvh_build": (C.c_int, [C.c_void_p, C.c_uint32]),
     "pt_renderer_set_traversal_limits": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32]),
     "pt_renderer_read_samples": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     "pt_bvh_build_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,

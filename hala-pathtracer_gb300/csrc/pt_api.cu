@@ -833,7 +833,8 @@ pt_status pt_renderer_commit(pt_renderer* r) {
     CK(r, bin.ensure(4 * (size_t)cap));
     BvhBuffers bb{bin.p, r->tri_sorted.p, cap};
     uint32_t nn = 0, nn4 = 0;
-    int rc = build_bvh(r->tri_v0.p, r->tri_e1.p, r->tri_e2.p, r->ntris, bb, &nn, st);
+    int rc = r->bvh_build == PT_BVH_BUILD_FAST ? build_bvh_fast(r->tri_v0.p, r->tri_e1.p, r->tri_e2.p, r->ntris, bb, &nn, st)
+                                               : build_bvh(r->tri_v0.p, r->tri_e1.p, r->tri_e2.p, r->ntris, bb, &nn, st);
     if (rc == 2) return fail(r, PT_ERR_OOM, "BVH build: out of device memory");
     if (rc != 0) return fail(r, PT_ERR_CUDA, "BVH build failed (code " + std::to_string(rc) + ")");
     CK(r, r->nodes.ensure(8 * (size_t)std::max<uint32_t>(nn, 1)));
@@ -1183,6 +1184,13 @@ pt_status pt_renderer_trace_rays(pt_renderer* r, const float* rays, uint32_t n, 
   CK(r, cudaMemcpyAsync(hits, dh.p, 16 * (size_t)n, cudaMemcpyDeviceToHost, r->stream));
   CK(r, cudaStreamSynchronize(r->stream));
   return check_traversal(r);
+}
+
+pt_status pt_renderer_set_bvh_build(pt_renderer* r, uint32_t mode) {
+  if (!r) return PT_ERR_INVALID_ARG;
+  if (mode != PT_BVH_BUILD_SAH && mode != PT_BVH_BUILD_FAST) return fail(r, PT_ERR_INVALID_ARG, "unknown BVH build");
+  r->bvh_build = mode;
+  return PT_OK;
 }
 
 pt_status pt_renderer_set_traversal_limits(pt_renderer* r, uint32_t stack_entries, uint32_t max_visits) {

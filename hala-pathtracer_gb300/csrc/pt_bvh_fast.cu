@@ -31,6 +31,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <utility>
 
 #include "pt_internal.h"
 
@@ -54,11 +55,6 @@ __global__ void k_fast_prep(const float4* v0, const float4* e1, const float4* e2
                             float4* thi, float4* tc, int* bounds) {
   __shared__ int red[FT / 32][12];
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  float v[12];
-  for (int k = 0; k < 6; ++k) {
-    v[k] = 1e30f;       // mins: centroid 0-2, box 6-8 (reordered below)
-    v[6 + k] = -1e30f;  // maxs
-  }
   float cmn[3] = {1e30f, 1e30f, 1e30f}, cmx[3] = {-1e30f, -1e30f, -1e30f};
   float bmn[3] = {1e30f, 1e30f, 1e30f}, bmx[3] = {-1e30f, -1e30f, -1e30f};
   if (i < n) {
@@ -81,7 +77,6 @@ __global__ void k_fast_prep(const float4* v0, const float4* e1, const float4* e2
     thi[i] = make_float4(hi[0], hi[1], hi[2], 0.0f);
     tc[i] = make_float4(c[0], c[1], c[2], 0.0f);
   }
-  (void)v;
   for (int o = 16; o > 0; o >>= 1)
     for (int k = 0; k < 3; ++k) {
       cmn[k] = fminf(cmn[k], __shfl_xor_sync(0xffffffffu, cmn[k], o));

@@ -189,6 +189,7 @@ struct pt_renderer {
   pt_stats stats{};
   uint32_t profiling = 0;
   std::vector<cudaEvent_t> tev;  // start/stop pairs around closest-hit launches
+  uint32_t bvh_build = PT_BVH_BUILD_SAH;  // pt_renderer_set_bvh_build
   // traversal limits and the device word their violations set (TRAV_ERR_*)
   uint32_t trav_stack = 96, trav_visits = 1u << 22;
   hpt::Buf<uint32_t> errw;

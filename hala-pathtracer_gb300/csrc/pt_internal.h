@@ -88,6 +88,10 @@ struct BvhBuffers {
 // Returns 0 on success; *num_nodes receives the number of nodes used.
 int build_bvh(const float4* tri_v0, const float4* tri_e1, const float4* tri_e2, uint32_t ntris, BvhBuffers& out,
               uint32_t* num_nodes, cudaStream_t st);
+// pt_bvh_fast.cu: the same output layout from a linear BVH over Morton codes
+// (fewer passes, no host round trip per level, a tree of lower quality).
+int build_bvh_fast(const float4* tri_v0, const float4* tri_e1, const float4* tri_e2, uint32_t ntris,
+                   BvhBuffers& out, uint32_t* num_nodes, cudaStream_t st);
 // Collapses the binary tree (64-B nodes) into 4-wide nodes (8 float4 each,
 // at most cap4 of them); *num_leaves (optional) receives the tree's leaf
 // count. Returns 0 on success.

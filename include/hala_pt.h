@@ -322,6 +322,17 @@ pt_status pt_renderer_get_stream(const pt_renderer* r, void** stream);
 pt_status pt_renderer_trace_rays(pt_renderer* r, const float* rays, uint32_t n,
                                  int32_t any_hit, int32_t brute_force, uint32_t* hits);
 
+/* BVH builder used by the next pt_renderer_commit (no counterpart in the
+ * reference, whose acceleration structures the Vulkan driver builds):
+ * PT_BVH_BUILD_SAH (default) prices binned SAH planes at every node, the
+ * tree that traces fastest; PT_BVH_BUILD_FAST builds a linear BVH over
+ * Morton codes in a fixed number of passes, for geometry rebuilt every
+ * frame. The images are the same either way (closest hits do not depend on
+ * the tree); only the build and traversal times differ. */
+#define PT_BVH_BUILD_SAH 0u
+#define PT_BVH_BUILD_FAST 1u
+pt_status pt_renderer_set_bvh_build(pt_renderer* r, uint32_t mode);
+
 /* Traversal limits of this renderer: stack entries per ray (1..96; 0 = 96)
  * and node visits per ray (0 = 2^22). A traversal that needs more stack than
  * `stack_entries` skips a subtree, and one that reaches `max_visits` stops;

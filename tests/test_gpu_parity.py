@@ -98,12 +98,14 @@ def test_bvh_large_scene_bitexact(pt, scenes, freq):
     assert np.array_equal(a[:, 3], b[:, 3])
 
 
-def test_bvh_degenerate_geometry(pt, scenes):
+@pytest.mark.parametrize("build", [0, 1])
+def test_bvh_degenerate_geometry(pt, scenes, build):
     """Inputs where no SAH plane separates the centroids, so every build tier
     falls back to median splits: 20,000 copies of one triangle (multi-block,
     one-block and whole-subtree tasks), 3,000 triangles in one plane, 600
     triangles sharing a centroid. Closest hits (equal distances resolved by
-    the lower id) and any-hit answers equal brute force."""
+    the lower id) and any-hit answers equal brute force, with the default
+    build and with the fast one (equal Morton codes ordered by index)."""
     sc = scenes.tiny_variants()["cornell"]
     sc.meshes = []
     sc.lights = []
@@ -120,7 +122,7 @@ def test_bvh_degenerate_geometry(pt, scenes):
     nested = np.concatenate([c + s * (tri - tri.mean(0)) for s in np.linspace(0.05, 1.5, 600)])
     n = np.zeros((1800, 3))
     sc.add_mesh(scenes.pack_vertices(nested, n, n, np.zeros((1800, 2))), np.arange(1800, dtype=np.uint32), mat)
-    r = pt.renderer_for(sc)
+    r = pt.renderer_for(sc, bvh_build=build)
     assert r.stats().triangles == 23600
     rays = _random_rays((np.zeros(3), np.ones(3)), 4000, 23)
     assert np.array_equal(r.trace_rays(rays), r.trace_rays(rays, brute_force=True))
@@ -271,3 +273,32 @@ def test_env_alias_tables_both_builders(pt, scenes, oracle_mod, size):
     rad_o, hash_o = o.trace_paths(np.arange(WH), 0, sc.spp)
     assert np.array_equal(hash_g, hash_o.reshape(-1))
     assert np.array_equal(rad_g.view(np.uint32), rad_o.reshape(-1, 3).view(np.uint32))
+
+
+@pytest.mark.parametrize("freq", [6, 72, 361])
+def test_fast_bvh_build_bitexact(pt, abi, scenes, freq):
+    """The fast builder (linear BVH over Morton codes, PT_BVH_BUILD_FAST) on
+    displaced icospheres of 722, 103,682 and 2,606,422 triangles plus the
+    ground quad (the oversized triangles take their own subtree): closest
+    hits and any-hit answers equal brute force, and a render equals the
+    default build's image bit for bit."""
+    sc = scenes.displaced_icosphere(48, 32, 2, freq=freq)
+    sc.lights = []
+    r = pt.renderer_for(sc, bvh_build=abi.BVH_BUILD_FAST)
+    st = r.stats()
+    assert st.triangles == sc.num_triangles and st.bvh_nodes > 0
+    rays = _random_rays(_bounds(sc), 4000, 31)
+    cam = np.array(sc.cameras[0].position, np.float32)
+    tgt = np.array([0.0, 0.0, 1.15]) + np.random.default_rng(32).uniform(-1.0, 1.0, size=(2000, 3))
+    rays[:2000, 0:3] = cam
+    dc = tgt - cam
+    rays[:2000, 4:7] = dc / np.linalg.norm(dc, axis=1, keepdims=True)
+    assert np.array_equal(r.trace_rays(rays), r.trace_rays(rays, brute_force=True))
+    rays[:, 7] = np.random.default_rng(33).uniform(0.01, 2.0, len(rays))
+    assert np.array_equal(r.trace_rays(rays, any_hit=True)[:, 3],
+                          r.trace_rays(rays, any_hit=True, brute_force=True)[:, 3])
+    r.render(sc.spp)
+    d = pt.renderer_for(sc)
+    d.render(sc.spp)
+    for k in (0, 1, 2, 3):
+        assert np.array_equal(r.image(k).view(np.uint8), d.image(k).view(np.uint8)), k
