@@ -193,6 +193,11 @@ class Renderer:
         """abi.BVH_BUILD_SAH (default) or abi.BVH_BUILD_FAST for the next commit()."""
         self._check(self._lib.pt_renderer_set_bvh_build(self._h, int(mode)))
 
+    def set_tail_paths(self, paths):
+        """Live paths at or below which a wave's remaining bounces run as one
+        kernel (0: never); the images do not depend on it."""
+        self._check(self._lib.pt_renderer_set_tail_paths(self._h, int(paths)))
+
     def set_traversal_limits(self, stack_entries=0, max_visits=0):
         """Traversal stack entries (1..96) and node visits per ray; 0 = default."""
         self._check(self._lib.pt_renderer_set_traversal_limits(self._h, int(stack_entries), int(max_visits)))

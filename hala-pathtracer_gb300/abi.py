@@ -209,6 +209,7 @@ RENDERER_SIGNATURES = {
                                          C.c_int32, C.c_int32, C.POINTER(C.c_uint32)]),
     "pt_renderer_set_bvh_build": (C.c_int, [C.c_void_p, C.c_uint32]),
     "pt_renderer_set_traversal_limits": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32]),
+    "pt_renderer_set_tail_paths": (C.c_int, [C.c_void_p, C.c_uint32]),
     "pt_renderer_read_samples": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     "pt_bvh_build_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
                                        C.c_uint32, C.c_void_p, C.POINTER(C.c_uint32), C.c_void_p,

@@ -131,7 +131,9 @@ cudaError_t run_bounces(const DevScene& S, WaveBuffers& W, uint32_t live, uint32
   }
   if (L.profiling == 0 && !L.host_loop) return run_bounces_graph(S, W, bounce_cap, L, pinned, st);
   const bool timing = (L.profiling & PT_PROFILE_TRACE_TIMING) != 0 && L.tev;
-  uint32_t b = 0;
+  const uint32_t tail = tail_paths(L, W);
+  uint32_t* tail_word = W.counters.p + 2 * Q_COUNT + G_TAIL;
+  uint32_t b = 0, tail_bounces = 0;
   for (; b < bounce_cap && live > 0; ++b) {
     uint32_t* out = (b & 1) ? cnt1 : cnt0;
     uint32_t* in_cnt = ((b & 1) ? cnt0 : cnt1) + Q_NEXT;
@@ -141,6 +143,21 @@ cudaError_t run_bounces(const DevScene& S, WaveBuffers& W, uint32_t live, uint32
     if (e != cudaSuccess) return e;
     QueueSet Q{qin, in_cnt, qnext, W.q_logic.p, W.q_diff.p, W.q_dis.p, W.q_glass.p, W.q_shadow.p, out,
                  W.rays.p};
+    if (live <= tail) {
+      // the rest of the wave in one kernel: the loop ends here
+      if ((e = cudaMemsetAsync(tail_word, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
+      launch_tail(S, W.P, Q, live, nullptr, b, bounce_cap, tail_word, st);
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+      if ((e = cudaMemcpyAsync(pinned, out + Q_NEXT, sizeof(uint32_t), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        return e;
+      if ((e = cudaMemcpyAsync(pinned + 1, tail_word, sizeof(uint32_t), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        return e;
+      if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+      live = pinned[0];
+      tail_bounces = pinned[1];
+      b += tail_bounces;
+      break;
+    }
     if (timing) {
       while (L.tev->size() < 2 * (L.ntimed + 1)) {
         cudaEvent_t ev;
@@ -163,7 +180,7 @@ cudaError_t run_bounces(const DevScene& S, WaveBuffers& W, uint32_t live, uint32
   }
   L.bounces = b;
   L.timed_out = live > 0;
-  L.launches = per_bounce * b;
+  L.launches = per_bounce * (b - tail_bounces) + (tail_bounces ? 1 : 0);
   return cudaSuccess;
 }
 
@@ -916,6 +933,7 @@ pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) {
   uint64_t launches = 0;
   BounceLoop L;
   L.profiling = r->profiling;
+  L.tail_paths = r->tail_paths;
   L.tev = &r->tev;
   const bool use_cache = r->cache_on;
   if (use_cache) {
@@ -1190,6 +1208,12 @@ pt_status pt_renderer_set_bvh_build(pt_renderer* r, uint32_t mode) {
   if (!r) return PT_ERR_INVALID_ARG;
   if (mode != PT_BVH_BUILD_SAH && mode != PT_BVH_BUILD_FAST) return fail(r, PT_ERR_INVALID_ARG, "unknown BVH build");
   r->bvh_build = mode;
+  return PT_OK;
+}
+
+pt_status pt_renderer_set_tail_paths(pt_renderer* r, uint32_t paths) {
+  if (!r) return PT_ERR_INVALID_ARG;
+  r->tail_paths = paths;
   return PT_OK;
 }
 

@@ -14,7 +14,12 @@
 // whether the loop goes on, so the host does one read-back per wave instead
 // of one per bounce. The loop ends when no path continues or after
 // `bounce_cap` bounces: every body iteration either runs a bounce (and
-// counts it) or ends the loop.
+// counts it) or ends the loop. The cases of the buckets of at most
+// `tail_paths` paths run the wave's tail instead of one bounce: one k_tail
+// launch that carries every remaining path to its end (as the host-driven
+// loop does once that few paths are left) and records the bounces it ran in
+// G_TAIL, which the next control kernel adds to the count and which ends
+// the loop.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -53,6 +58,7 @@ __global__ void k_graph_init(uint32_t* gctl, const uint32_t* cnt_odd, uint32_t* 
   gctl[G_DONE] = 0;
   gctl[G_LIVE] = live;
   gctl[G_GO] = go ? 1u : 0u;
+  gctl[G_TAIL] = 0;
   cudaGraphSetConditional(h_first, go ? bucket_of(live, nb) : nb);
   cudaGraphSetConditional(h_loop, go ? 1u : 0u);
 }
@@ -64,9 +70,10 @@ __global__ void k_graph_step(uint32_t* gctl, const uint32_t* cnt_this, uint32_t*
                              uint32_t cap, cudaGraphConditionalHandle h_next, cudaGraphConditionalHandle h_loop,
                              int last) {
   bool go = false;
-  if (gctl[G_GO]) {  // the bounce before this kernel ran
+  if (gctl[G_GO]) {  // the bounce before this kernel ran (or the wave's tail, G_TAIL bounces)
     const uint32_t live = cnt_this[Q_NEXT];
-    const uint32_t done = gctl[G_DONE] + 1u;
+    const uint32_t tail = gctl[G_TAIL];
+    const uint32_t done = gctl[G_DONE] + (tail ? tail : 1u);
     go = live > 0 && done < cap;
     for (int k = 0; k < Q_COUNT; ++k) cnt_other[k] = 0;
     gctl[G_DONE] = done;
@@ -96,7 +103,7 @@ void append(std::vector<unsigned char>& k, const void* p, size_t n) {
 }
 
 // Everything the captured kernels received by value, plus the graph shape.
-std::vector<unsigned char> graph_key(const DevScene& S, WaveBuffers& W, uint32_t bounce_cap) {
+std::vector<unsigned char> graph_key(const DevScene& S, WaveBuffers& W, uint32_t bounce_cap, uint32_t tail) {
   std::vector<unsigned char> k;
   append(k, &S, sizeof(S));
   append(k, &W.P, sizeof(W.P));
@@ -104,7 +111,7 @@ std::vector<unsigned char> graph_key(const DevScene& S, WaveBuffers& W, uint32_t
     const QueueSet Q = queues_for(W, parity);
     append(k, &Q, sizeof(Q));
   }
-  const uint32_t shape[2] = {W.cap, bounce_cap};
+  const uint32_t shape[3] = {W.cap, bounce_cap, tail};
   append(k, shape, sizeof(shape));
   return k;
 }
@@ -121,7 +128,8 @@ cudaError_t add_kernel_node(cudaGraphNode_t* node, cudaGraph_t g, const cudaGrap
   return cudaGraphAddKernelNode(node, g, dep, dep ? 1 : 0, &kp);
 }
 
-cudaError_t build_graph(const DevScene& S, WaveBuffers& W, uint32_t bounce_cap, cudaStream_t st, cudaGraph_t* out) {
+cudaError_t build_graph(const DevScene& S, WaveBuffers& W, uint32_t bounce_cap, uint32_t tail, cudaStream_t st,
+                        cudaGraph_t* out) {
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaGraphCreate(&g, 0);
   if (e != cudaSuccess) return e;
@@ -170,8 +178,13 @@ cudaError_t build_graph(const DevScene& S, WaveBuffers& W, uint32_t bounce_cap, 
           cudaSuccess)
         return fail(e);
       const uint32_t lim = bucket_limit(k, nb, W.cap);
-      launch_trace(S, W.P, Q, lim, false, st);
-      launch_shade(S, W.P, Q, lim, st);
+      if (lim <= tail) {
+        // few paths left: the rest of the wave in one kernel
+        launch_tail(S, W.P, Q, lim, gctl + G_DONE, 0u, bounce_cap, gctl + G_TAIL, st);
+      } else {
+        launch_trace(S, W.P, Q, lim, false, st);
+        launch_shade(S, W.P, Q, lim, st);
+      }
       cudaError_t le = cudaGetLastError();
       cudaGraph_t captured = nullptr;
       e = cudaStreamEndCapture(st, &captured);
@@ -204,11 +217,12 @@ void BounceGraph::reset() {
 cudaError_t run_bounces_graph(const DevScene& S, WaveBuffers& W, uint32_t bounce_cap, BounceLoop& L,
                               uint32_t* pinned, cudaStream_t st) {
   BounceGraph& G = W.graph;
-  std::vector<unsigned char> key = graph_key(S, W, bounce_cap);
+  const uint32_t tail = tail_paths(L, W);
+  std::vector<unsigned char> key = graph_key(S, W, bounce_cap, tail);
   cudaError_t e;
   if (!G.exec || key != G.key) {
     cudaGraph_t g = nullptr;
-    if ((e = build_graph(S, W, bounce_cap, st, &g)) != cudaSuccess) {
+    if ((e = build_graph(S, W, bounce_cap, tail, st, &g)) != cudaSuccess) {
       G.reset();
       return e;
     }
@@ -233,15 +247,17 @@ cudaError_t run_bounces_graph(const DevScene& S, WaveBuffers& W, uint32_t bounce
     ++G.builds;
   }
   if ((e = cudaGraphLaunch(G.exec, st)) != cudaSuccess) return e;
-  if ((e = cudaMemcpyAsync(pinned, W.counters.p + 2 * Q_COUNT, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st)) !=
-      cudaSuccess)
+  if ((e = cudaMemcpyAsync(pinned, W.counters.p + 2 * Q_COUNT, G_WORDS * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                           st)) != cudaSuccess)
     return e;
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
-  const uint32_t done = pinned[G_DONE], live = pinned[G_LIVE];
+  const uint32_t done = pinned[G_DONE], live = pinned[G_LIVE], tail_bounces = pinned[G_TAIL];
   const uint64_t per_bounce = (S.features & PT_FEATURE_MEDIUM) ? 5 : 6;
+  const uint64_t cases = done - tail_bounces + (tail_bounces ? 1 : 0);  // switch cases that ran
   L.bounces = done;
   L.timed_out = live > 0;
-  L.launches = per_bounce * done + 1 + 2ull * ((done + 1) / 2);  // bounces, init, two control kernels per iteration
+  // bounces, the tail, init, two control kernels per loop iteration
+  L.launches = per_bounce * (done - tail_bounces) + (tail_bounces ? 1 : 0) + 1 + 2ull * ((cases + 1) / 2);
   return cudaSuccess;
 }
 

@@ -112,6 +112,7 @@ struct BounceLoop {
   uint32_t bounces = 0;              // bounces run by the last wave
   bool timed_out = false;            // paths still alive after the bounce cap
   uint64_t launches = 0;             // kernels launched by the last wave's bounces
+  uint32_t tail_paths = 4096;        // live paths at or below which the rest of a wave is one k_tail launch
 };
 
 // Runs bounce after bounce of the `live` paths queued in W.q_a (the camera
@@ -125,7 +126,17 @@ cudaError_t run_bounces(const DevScene& S, WaveBuffers& W, uint32_t live, uint32
 
 // The graph form of run_bounces (pt_graph.cu). Control words live after the
 // two counter sets: counters[2 * Q_COUNT + G_*].
-enum GraphWord : uint32_t { G_DONE = 0, G_LIVE = 1, G_GO = 2, G_WORDS = 4 };
+// G_TAIL: the most bounces a path ran in the wave's k_tail launch (0 before it).
+enum GraphWord : uint32_t { G_DONE = 0, G_LIVE = 1, G_GO = 2, G_TAIL = 3, G_WORDS = 4 };
+
+// The wave-tail threshold in effect: none for radiance-cache waves (their
+// training appends follow the wavefront's queue order) and under the
+// traversal-timing or counting instrumentation (which instruments the
+// wavefront's closest-hit launches).
+inline uint32_t tail_paths(const BounceLoop& L, const WaveBuffers& W) {
+  if ((L.profiling & (PT_PROFILE_TRACE_TIMING | PT_PROFILE_COUNT)) != 0 || W.P.c_rec != nullptr) return 0;
+  return L.tail_paths;
+}
 cudaError_t run_bounces_graph(const DevScene& S, WaveBuffers& W, uint32_t bounce_cap, BounceLoop& L,
                               uint32_t* pinned, cudaStream_t st);
 
@@ -190,6 +201,7 @@ struct pt_renderer {
   uint32_t profiling = 0;
   std::vector<cudaEvent_t> tev;  // start/stop pairs around closest-hit launches
   uint32_t bvh_build = PT_BVH_BUILD_SAH;  // pt_renderer_set_bvh_build
+  uint32_t tail_paths = 4096;              // pt_renderer_set_tail_paths
   // traversal limits and the device word their violations set (TRAV_ERR_*)
   uint32_t trav_stack = 96, trav_visits = 1u << 22;
   hpt::Buf<uint32_t> errw;

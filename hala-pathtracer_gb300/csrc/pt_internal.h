@@ -44,6 +44,24 @@ void launch_materials_multi(const DevScene& S, const PathState& P, const QueueSe
                             cudaStream_t st);
 void launch_materials_multi_medium(const DevScene& S, const PathState& P, const QueueSet& Q, int grid, bool tr,
                                    bool tex, cudaStream_t st);
+// The tail of a wave: every remaining bounce of the paths queued in Q.in,
+// one thread per path (k_tail in pt_shade.cuh), at most `cap` bounces in
+// the wave counting the `done` (or *done_ptr) already run; the most bounces
+// a path ran goes to *tail_bounces (atomicMax). Not for radiance-cache waves.
+void launch_tail(const DevScene& S, const PathState& P, const QueueSet& Q, uint32_t max_items,
+                 const uint32_t* done_ptr, uint32_t done, uint32_t cap, uint32_t* tail_bounces, cudaStream_t st);
+void launch_tail_plain(const DevScene& S, const PathState& P, const QueueSet& Q, uint32_t max_items,
+                       const uint32_t* done_ptr, uint32_t done, uint32_t cap, uint32_t* tail_bounces, bool tr, bool tex,
+                       cudaStream_t st);
+void launch_tail_medium(const DevScene& S, const PathState& P, const QueueSet& Q, uint32_t max_items,
+                        const uint32_t* done_ptr, uint32_t done, uint32_t cap, uint32_t* tail_bounces, bool tr, bool tex,
+                        cudaStream_t st);
+void launch_tail_multi(const DevScene& S, const PathState& P, const QueueSet& Q, uint32_t max_items,
+                       const uint32_t* done_ptr, uint32_t done, uint32_t cap, uint32_t* tail_bounces, bool tr, bool tex,
+                       cudaStream_t st);
+void launch_tail_multi_medium(const DevScene& S, const PathState& P, const QueueSet& Q, uint32_t max_items,
+                              const uint32_t* done_ptr, uint32_t done, uint32_t cap, uint32_t* tail_bounces, bool tr,
+                              bool tex, cudaStream_t st);
 void launch_camera_multi(const PathState& P, const WaveSegment* segs, uint32_t nseg, uint32_t n, uint32_t* q_active,
                          uint32_t* active_count, cudaStream_t st);
 void launch_accumulate(const PathState& P, uint64_t g0, uint32_t n, uint32_t WH, float4* accum, float4* albedo,

@@ -120,22 +120,8 @@ __global__ void __launch_bounds__(TRACE_BLOCK, 5) k_trace(const __grid_constant_
   const uint32_t n = *Q.in_count;
   TravCount tc;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    uint32_t p = Q.in[i];
-    const DevScene& S = MULTI ? P.jobs[P.job[p]] : S0;
-    if (P.c_train) {
-      // a training path leaving the cache vertex: what it gathered so far is
-      // the part of its radiance the cache does not predict
-      uint32_t k = P.c_train[p];
-      if (k != 0xFFFFFFFFu && P.depth[p] == P.c_depth + 1u) P.t_R[k] = P.rad[p];
-    }
-    float4 o4 = P.ray_o[p], d4 = P.ray_d[p];
-    HitRec h = trace_closest<BRUTE, COUNT>(S, f3(o4), f3(d4), 0.0f, WORLD_SIZE, &tc);
-    P.hit[p] = make_float4(h.t, h.u, h.v, __uint_as_float(h.id));
-    uint32_t cls = 0;  // surface logic, else MAT_CLASS_*
-    if (h.id != HIT_MISS && !(h.id & HIT_LIGHT_BIT)) {
-      uint32_t m = __ldg(&S.tri_mat[h.id]);
-      if (m < S.num_mats) cls = __ldg(&S.mat_class[m]);
-    }
+    const uint32_t p = Q.in[i];
+    const uint32_t cls = trace_path<BRUTE, COUNT, MULTI>(S0, P, p, tc);
     queue_push(Q.logic, &Q.counts[Q_LOGIC], p, cls == 0);
     queue_push(Q.diffuse, &Q.counts[Q_DIFFUSE], p, cls == MAT_CLASS_DIFFUSE);
     queue_push(Q.disney, &Q.counts[Q_DISNEY], p, cls == MAT_CLASS_DISNEY);
@@ -149,41 +135,11 @@ __global__ void __launch_bounds__(TRACE_BLOCK, 5) k_trace(const __grid_constant_
 }
 
 // ------------------------------------------------------------------ shadow rays
-// inc/lighting.glsl:116-149 and :203-238 (visibility + radiance += T * Ld)
 template <bool BRUTE, bool MULTI>
 __global__ void __launch_bounds__(256, 5) k_shadow(const __grid_constant__ DevScene S0, PathState P, QueueSet Q) {
   const uint32_t n = Q.counts[Q_SHADOW];
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    uint32_t p = Q.shadow[i];
-    const DevScene& S = MULTI ? P.jobs[P.job[p]] : S0;
-    float4 so = P.sh_o[p];
-    uint32_t pend = __float_as_uint(so.w);
-    float3 o = f3(so);
-    float4 r4 = P.rad[p];
-    uint32_t hash = __float_as_uint(r4.w);
-    float3 Ld = f3(0.0f);
-    uint32_t nrays = 0;
-    if (pend & PEND_ENV) {
-      float4 d0 = P.sh_d0[p];
-      bool occ = trace_any<BRUTE>(S, o, f3(d0), 0.0f, d0.w);
-      ++nrays;
-      hmix(hash, 0x40000000u | (occ ? 0u : 1u));
-      if (!occ) Ld += f3(P.sh_c0[p]);
-    }
-    if (pend & PEND_LIGHT) {
-      float4 d1 = P.sh_d1[p];
-      bool occ = trace_any<BRUTE>(S, o, f3(d1), 0.0f, d1.w);
-      ++nrays;
-      hmix(hash, 0x50000000u | (occ ? 0u : 1u));
-      if (!occ) Ld += f3(P.sh_c1[p]);
-    }
-    if (pend & PEND_BSDF) hmix(hash, 0x60000000u | ((pend >> 8) & 0xFFFu));
-    if (pend & PEND_STOP) hmix(hash, 0x61000000u);
-    if (pend & PEND_RR) hmix(hash, 0x72000000u);
-    float3 rad = f3(r4) + f3(P.sh_T[p]) * Ld;
-    P.rad[p] = make_float4(rad.x, rad.y, rad.z, __uint_as_float(hash));
-    count_add(&Q.rays[1], nrays);
-  }
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    count_add(&Q.rays[1], shadow_path<BRUTE, MULTI>(S0, P, Q.shadow[i]));
 }
 
 // ------------------------------------------------------------------ accumulation
@@ -320,6 +276,20 @@ void launch_shade(const DevScene& S, const PathState& P, const QueueSet& Q, uint
     else if (P.c_rec != nullptr) launch_materials_cache(S, P, Q, g, tr, tex, st);
     else launch_materials_plain(S, P, Q, g, tr, tex, st);
     if (!med) k_shadow<false, false><<<g, 256, 0, st>>>(S, P, Q);
+  }
+}
+
+void launch_tail(const DevScene& S, const PathState& P, const QueueSet& Q, uint32_t max_items,
+                 const uint32_t* done_ptr, uint32_t done, uint32_t cap, uint32_t* tail_bounces, cudaStream_t st) {
+  const bool med = (S.features & PT_FEATURE_MEDIUM) != 0;
+  const bool tr = (S.features & PT_FEATURE_TRANSPARENT) != 0;
+  const bool tex = (S.features & PT_FEATURE_TEXTURED) != 0;
+  if (P.job) {
+    if (med) launch_tail_multi_medium(S, P, Q, max_items, done_ptr, done, cap, tail_bounces, tr, tex, st);
+    else launch_tail_multi(S, P, Q, max_items, done_ptr, done, cap, tail_bounces, tr, tex, st);
+  } else {
+    if (med) launch_tail_medium(S, P, Q, max_items, done_ptr, done, cap, tail_bounces, tr, tex, st);
+    else launch_tail_plain(S, P, Q, max_items, done_ptr, done, cap, tail_bounces, tr, tex, st);
   }
 }
 

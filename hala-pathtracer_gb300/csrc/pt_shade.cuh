@@ -5,6 +5,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "pt_internal.h"
 #include "pt_trace.cuh"
 
@@ -275,10 +277,8 @@ __device__ __forceinline__ float4 sample_texture(const DevScene& S, uint32_t t, 
 // ------------------------------------------------------------------ miss / emitter / invalid
 // pathtracer.rgen.glsl:70-115
 template <bool MULTI>
-__global__ void __launch_bounds__(256) k_shade_logic(const __grid_constant__ DevScene S0, PathState P, QueueSet Q) {
-  const uint32_t n = Q.counts[Q_LOGIC];
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    uint32_t p = Q.logic[i];
+__device__ __forceinline__ void logic_path(const DevScene& S0, const PathState& P, uint32_t p) {
+  {
     const DevScene& S = MULTI ? P.jobs[P.job[p]] : S0;
     float4 h = P.hit[p];
     uint32_t id = __float_as_uint(h.w);
@@ -306,6 +306,13 @@ __global__ void __launch_bounds__(256) k_shade_logic(const __grid_constant__ Dev
     }
     P.rad[p] = make_float4(rad.x, rad.y, rad.z, __uint_as_float(hash));
   }
+}
+
+template <bool MULTI>
+__global__ void __launch_bounds__(256) k_shade_logic(const __grid_constant__ DevScene S0, PathState P, QueueSet Q) {
+  const uint32_t n = Q.counts[Q_LOGIC];
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    logic_path<MULTI>(S0, P, Q.logic[i]);
 }
 
 // ------------------------------------------------------------------ surface shading
@@ -412,6 +419,64 @@ struct Shader {
 // the visibility events, in the reference's order).
 constexpr uint32_t PEND_ENV = 1u, PEND_LIGHT = 2u, PEND_BSDF = 4u, PEND_STOP = 8u, PEND_RR = 16u;
 
+// Closest hit of path p's ray and the class of what it hit: 0 for a miss,
+// an emitter or an invalid material (surface logic), else MAT_CLASS_*
+// (pathtracer.rgen.glsl:56-68, triangles.rchit.glsl:13-76).
+template <bool BRUTE, bool COUNT, bool MULTI>
+__device__ __forceinline__ uint32_t trace_path(const DevScene& S0, const PathState& P, uint32_t p, TravCount& tc) {
+  const DevScene& S = MULTI ? P.jobs[P.job[p]] : S0;
+  if (P.c_train) {
+    // a training path leaving the cache vertex: what it gathered so far is
+    // the part of its radiance the cache does not predict
+    uint32_t k = P.c_train[p];
+    if (k != 0xFFFFFFFFu && P.depth[p] == P.c_depth + 1u) P.t_R[k] = P.rad[p];
+  }
+  float4 o4 = P.ray_o[p], d4 = P.ray_d[p];
+  HitRec h = trace_closest<BRUTE, COUNT>(S, f3(o4), f3(d4), 0.0f, WORLD_SIZE, &tc);
+  P.hit[p] = make_float4(h.t, h.u, h.v, __uint_as_float(h.id));
+  uint32_t cls = 0;
+  if (h.id != HIT_MISS && !(h.id & HIT_LIGHT_BIT)) {
+    uint32_t m = __ldg(&S.tri_mat[h.id]);
+    if (m < S.num_mats) cls = __ldg(&S.mat_class[m]);
+  }
+  return cls;
+}
+
+// The deferred shadow rays of path p and the hash events that wait for
+// them (inc/lighting.glsl:116-149 and :203-238: visibility, then
+// radiance += T * Ld). Returns the number of rays traced.
+template <bool BRUTE, bool MULTI>
+__device__ __forceinline__ uint32_t shadow_path(const DevScene& S0, const PathState& P, uint32_t p) {
+  const DevScene& S = MULTI ? P.jobs[P.job[p]] : S0;
+  float4 so = P.sh_o[p];
+  uint32_t pend = __float_as_uint(so.w);
+  float3 o = f3(so);
+  float4 r4 = P.rad[p];
+  uint32_t hash = __float_as_uint(r4.w);
+  float3 Ld = f3(0.0f);
+  uint32_t nrays = 0;
+  if (pend & PEND_ENV) {
+    float4 d0 = P.sh_d0[p];
+    bool occ = trace_any<BRUTE>(S, o, f3(d0), 0.0f, d0.w);
+    ++nrays;
+    hmix(hash, 0x40000000u | (occ ? 0u : 1u));
+    if (!occ) Ld += f3(P.sh_c0[p]);
+  }
+  if (pend & PEND_LIGHT) {
+    float4 d1 = P.sh_d1[p];
+    bool occ = trace_any<BRUTE>(S, o, f3(d1), 0.0f, d1.w);
+    ++nrays;
+    hmix(hash, 0x50000000u | (occ ? 0u : 1u));
+    if (!occ) Ld += f3(P.sh_c1[p]);
+  }
+  if (pend & PEND_BSDF) hmix(hash, 0x60000000u | ((pend >> 8) & 0xFFFu));
+  if (pend & PEND_STOP) hmix(hash, 0x61000000u);
+  if (pend & PEND_RR) hmix(hash, 0x72000000u);
+  float3 rad = f3(r4) + f3(P.sh_T[p]) * Ld;
+  P.rad[p] = make_float4(rad.x, rad.y, rad.z, __uint_as_float(hash));
+  return nrays;
+}
+
 // Warp-aggregated append that returns the slot index (or ~0u when !pred).
 __device__ __forceinline__ uint32_t append_index(uint32_t* counter, bool pred) {
   unsigned active = __activemask();
@@ -455,14 +520,17 @@ __device__ __forceinline__ void apply_maps(const DevScene& S, pt_material& m, Su
   }
 }
 
-template <int MAT, bool MEDIUM, bool TRANSPARENT, bool MULTI, bool CACHE = false, bool TEXTURED = false>
-__global__ void __launch_bounds__(256, MEDIUM ? 4 : 3) k_shade(const __grid_constant__ DevScene S0, PathState P, QueueSet Q) {
-  const int slot = MAT == SHADE_DISNEY_GLASS ? Q_GLASS : (MAT == PT_MATERIAL_DISNEY ? Q_DISNEY : Q_DIFFUSE);
-  const uint32_t* qin = MAT == SHADE_DISNEY_GLASS ? Q.glass : (MAT == PT_MATERIAL_DISNEY ? Q.disney : Q.diffuse);
-  const uint32_t n = Q.counts[slot];
-  unsigned long long nshadow_total = 0;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    uint32_t p = qin[i];
+// What one shading step decided for its path: the path ends (`stop`), and
+// its shadow rays and pending hash events wait for k_shadow (`deferred`).
+struct ShadeResult {
+  bool stop, deferred;
+};
+
+// One surface (or medium) vertex of path p: pathtracer.rgen.glsl:117-256.
+template <int MAT, bool MEDIUM, bool TRANSPARENT, bool MULTI, bool CACHE, bool TEXTURED>
+__device__ __forceinline__ ShadeResult shade_path(const DevScene& S0, const PathState& P, uint32_t p,
+                                                  unsigned long long& nshadow_total) {
+  {
     const DevScene& S = MULTI ? P.jobs[P.job[p]] : S0;
     Shader<MAT> sh{S, P.rng[p], 0u, 0ull};
     float4 h = P.hit[p];
@@ -704,11 +772,104 @@ __global__ void __launch_bounds__(256, MEDIUM ? 4 : 3) k_shade(const __grid_cons
       so.w = __uint_as_float(pend);
       P.sh_o[p] = so;
     }
-    queue_push(Q.shadow, &Q.counts[Q_SHADOW], p, deferred);
-    queue_push(Q.next, &Q.counts[Q_NEXT], p, !stop);
     nshadow_total += sh.nshadow;
+    return ShadeResult{stop, deferred};
+  }
+}
+
+template <int MAT, bool MEDIUM, bool TRANSPARENT, bool MULTI, bool CACHE = false, bool TEXTURED = false>
+__global__ void __launch_bounds__(256, MEDIUM ? 4 : 3) k_shade(const __grid_constant__ DevScene S0, PathState P, QueueSet Q) {
+  const int slot = MAT == SHADE_DISNEY_GLASS ? Q_GLASS : (MAT == PT_MATERIAL_DISNEY ? Q_DISNEY : Q_DIFFUSE);
+  const uint32_t* qin = MAT == SHADE_DISNEY_GLASS ? Q.glass : (MAT == PT_MATERIAL_DISNEY ? Q.disney : Q.diffuse);
+  const uint32_t n = Q.counts[slot];
+  unsigned long long nshadow_total = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t p = qin[i];
+    const ShadeResult r = shade_path<MAT, MEDIUM, TRANSPARENT, MULTI, CACHE, TEXTURED>(S0, P, p, nshadow_total);
+    queue_push(Q.shadow, &Q.counts[Q_SHADOW], p, r.deferred);
+    queue_push(Q.next, &Q.counts[Q_NEXT], p, !r.stop);
   }
   if (MEDIUM) count_add(&Q.rays[1], (uint32_t)nshadow_total);
+}
+
+// ------------------------------------------------------------------ wave tail
+// Once few paths are left in a wave, every remaining bounce of the wavefront
+// loop costs about the latency of its slowest ray and its slowest shading
+// call (measured on the GB300: ~140 us per bounce for 256 paths of the
+// Disney grid, whatever their number), so the tail of a wave runs as one
+// kernel in which each thread carries its path to the end: closest hit,
+// surface logic or shading, shadow rays, again. Each step is the same device
+// function the wavefront kernels call, in the same order per path, so every
+// path's radiance, albedo, normal and hit-sequence hash are bit-identical to
+// the wavefront's; only the schedule differs.
+constexpr uint32_t TAIL_BLOCK = 64;  // small blocks spread the few paths over many SMs
+
+template <int MAT, bool MEDIUM, bool TRANSPARENT, bool MULTI, bool TEXTURED>
+__device__ __noinline__ ShadeResult tail_shade(const DevScene& S0, const PathState& P, uint32_t p,
+                                               unsigned long long& nshadow) {
+  return shade_path<MAT, MEDIUM, TRANSPARENT, MULTI, false, TEXTURED>(S0, P, p, nshadow);
+}
+
+// Paths queued in Q.in run at most `cap - done` more bounces, `done` being
+// the bounces the wave already ran (*done_ptr when given, else `done`). A
+// path still alive after that is appended to Q.next (the bounce cap was
+// reached). The most bounces any path ran goes to *tail_bounces (atomicMax),
+// the rays to Q.rays[0] / Q.rays[1].
+template <bool MEDIUM, bool TRANSPARENT, bool MULTI, bool TEXTURED>
+__global__ void __launch_bounds__(TAIL_BLOCK) k_tail(const __grid_constant__ DevScene S0, PathState P, QueueSet Q,
+                                                     const uint32_t* done_ptr, uint32_t done, uint32_t cap,
+                                                     uint32_t* tail_bounces) {
+  const uint32_t n = *Q.in_count;
+  const uint32_t d0 = done_ptr ? *done_ptr : done;
+  const uint32_t budget = cap > d0 ? cap - d0 : 0u;
+  unsigned long long nclosest = 0, nshadow = 0;
+  uint32_t most = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t p = Q.in[i];
+    bool live = true;
+    uint32_t it = 0;
+    while (live && it < budget) {
+      ++it;
+      TravCount tc;
+      const uint32_t cls = trace_path<false, false, MULTI>(S0, P, p, tc);
+      ++nclosest;
+      if (cls == 0) {
+        logic_path<MULTI>(S0, P, p);
+        live = false;
+      } else {
+        ShadeResult r;
+        if (cls == MAT_CLASS_DIFFUSE)
+          r = tail_shade<PT_MATERIAL_DIFFUSE, MEDIUM, TRANSPARENT, MULTI, TEXTURED>(S0, P, p, nshadow);
+        else if (cls == MAT_CLASS_DISNEY)
+          r = tail_shade<PT_MATERIAL_DISNEY, MEDIUM, TRANSPARENT, MULTI, TEXTURED>(S0, P, p, nshadow);
+        else
+          r = tail_shade<SHADE_DISNEY_GLASS, MEDIUM, TRANSPARENT, MULTI, TEXTURED>(S0, P, p, nshadow);
+        if (r.deferred) nshadow += shadow_path<false, MULTI>(S0, P, p);
+        live = !r.stop;
+      }
+    }
+    most = max(most, it);
+    queue_push(Q.next, &Q.counts[Q_NEXT], p, live);
+  }
+  count_add(&Q.rays[0], (uint32_t)nclosest);
+  count_add(&Q.rays[1], (uint32_t)nshadow);
+  const unsigned active = __activemask();
+  most = __reduce_max_sync(active, most);
+  if ((int)lane_id() == __ffs(active) - 1 && most) atomicMax(tail_bounces, most);
+}
+
+template <bool MED, bool MULTI>
+inline void launch_tail_permutation(const DevScene& S, const PathState& P, const QueueSet& Q, uint32_t max_items,
+                                    const uint32_t* done_ptr, uint32_t done, uint32_t cap, uint32_t* tail_bounces,
+                                    bool tr, bool tex, cudaStream_t st) {
+  const int g = (int)std::max<uint32_t>(1u, (max_items + TAIL_BLOCK - 1) / TAIL_BLOCK);
+  if (tr) {
+    if (tex) k_tail<MED, true, MULTI, true><<<g, TAIL_BLOCK, 0, st>>>(S, P, Q, done_ptr, done, cap, tail_bounces);
+    else k_tail<MED, true, MULTI, false><<<g, TAIL_BLOCK, 0, st>>>(S, P, Q, done_ptr, done, cap, tail_bounces);
+  } else {
+    if (tex) k_tail<MED, false, MULTI, true><<<g, TAIL_BLOCK, 0, st>>>(S, P, Q, done_ptr, done, cap, tail_bounces);
+    else k_tail<MED, false, MULTI, false><<<g, TAIL_BLOCK, 0, st>>>(S, P, Q, done_ptr, done, cap, tail_bounces);
+  }
 }
 
 // The three material kernels of one bounce (diffuse, opaque Disney, Disney

@@ -333,6 +333,15 @@ pt_status pt_renderer_trace_rays(pt_renderer* r, const float* rays, uint32_t n,
 #define PT_BVH_BUILD_FAST 1u
 pt_status pt_renderer_set_bvh_build(pt_renderer* r, uint32_t mode);
 
+/* Wave tail (no counterpart in the reference): once at most `paths` paths
+ * of a wavefront are still alive, their remaining bounces run as one kernel
+ * launch, one thread carrying each path to its end, instead of one launch
+ * chain per bounce whose time the slowest ray sets. 0 turns it off; the
+ * default is 4096. Images, ray counts and bounce counts are the same either
+ * way. Radiance-cache renders and the PT_PROFILE_TRACE_TIMING /
+ * PT_PROFILE_COUNT instrumentation always use the per-bounce launches. */
+pt_status pt_renderer_set_tail_paths(pt_renderer* r, uint32_t paths);
+
 /* Traversal limits of this renderer: stack entries per ray (1..96; 0 = 96)
  * and node visits per ray (0 = 2^22). A traversal that needs more stack than
  * `stack_entries` skips a subtree, and one that reaches `max_visits` stops;
