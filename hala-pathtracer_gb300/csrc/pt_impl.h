@@ -112,7 +112,7 @@ struct BounceLoop {
   uint32_t bounces = 0;              // bounces run by the last wave
   bool timed_out = false;            // paths still alive after the bounce cap
   uint64_t launches = 0;             // kernels launched by the last wave's bounces
-  uint32_t tail_paths = 4096;        // live paths at or below which the rest of a wave is one k_tail launch
+  uint32_t tail_paths = 16384;       // live paths at or below which the rest of a wave is one k_tail launch
 };
 
 // Runs bounce after bounce of the `live` paths queued in W.q_a (the camera
@@ -201,7 +201,7 @@ struct pt_renderer {
   uint32_t profiling = 0;
   std::vector<cudaEvent_t> tev;  // start/stop pairs around closest-hit launches
   uint32_t bvh_build = PT_BVH_BUILD_SAH;  // pt_renderer_set_bvh_build
-  uint32_t tail_paths = 4096;              // pt_renderer_set_tail_paths
+  uint32_t tail_paths = 16384;             // pt_renderer_set_tail_paths
   // traversal limits and the device word their violations set (TRAV_ERR_*)
   uint32_t trav_stack = 96, trav_visits = 1u << 22;
   hpt::Buf<uint32_t> errw;

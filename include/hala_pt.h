@@ -337,7 +337,9 @@ pt_status pt_renderer_set_bvh_build(pt_renderer* r, uint32_t mode);
  * of a wavefront are still alive, their remaining bounces run as one kernel
  * launch, one thread carrying each path to its end, instead of one launch
  * chain per bounce whose time the slowest ray sets. 0 turns it off; the
- * default is 4096. Images, ray counts and bounce counts are the same either
+ * default is 16384. The bounce graph switches at its grid sizes (4096 x 4^k
+ * paths), so the threshold in effect there is the largest such size not
+ * above `paths`. Images, ray counts and bounce counts are the same either
  * way. Radiance-cache renders and the PT_PROFILE_TRACE_TIMING /
  * PT_PROFILE_COUNT instrumentation always use the per-bounce launches. */
 pt_status pt_renderer_set_tail_paths(pt_renderer* r, uint32_t paths);
