@@ -934,6 +934,11 @@ pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) {
   BounceLoop L;
   L.profiling = r->profiling;
   L.tail_paths = r->tail_paths;
+  // With a radiance cache, the paths that go on past the cache vertex are
+  // the 1 in 2^train_shift that train it: the tail takes over once only
+  // they are left.
+  if (r->cache_on && L.tail_paths > 0)
+    L.tail_paths = std::max<uint32_t>(L.tail_paths, (uint32_t)(r->cache_cfg.paths_per_pass >> r->cache_cfg.train_shift));
   L.tev = &r->tev;
   const bool use_cache = r->cache_on;
   if (use_cache) {

@@ -129,12 +129,11 @@ cudaError_t run_bounces(const DevScene& S, WaveBuffers& W, uint32_t live, uint32
 // G_TAIL: the most bounces a path ran in the wave's k_tail launch (0 before it).
 enum GraphWord : uint32_t { G_DONE = 0, G_LIVE = 1, G_GO = 2, G_TAIL = 3, G_WORDS = 4 };
 
-// The wave-tail threshold in effect: none for radiance-cache waves (their
-// training appends follow the wavefront's queue order) and under the
-// traversal-timing or counting instrumentation (which instruments the
-// wavefront's closest-hit launches).
-inline uint32_t tail_paths(const BounceLoop& L, const WaveBuffers& W) {
-  if ((L.profiling & (PT_PROFILE_TRACE_TIMING | PT_PROFILE_COUNT)) != 0 || W.P.c_rec != nullptr) return 0;
+// The wave-tail threshold in effect: none under the traversal-timing or
+// counting instrumentation (which instruments the wavefront's closest-hit
+// launches).
+inline uint32_t tail_paths(const BounceLoop& L, const WaveBuffers&) {
+  if ((L.profiling & (PT_PROFILE_TRACE_TIMING | PT_PROFILE_COUNT)) != 0) return 0;
   return L.tail_paths;
 }
 cudaError_t run_bounces_graph(const DevScene& S, WaveBuffers& W, uint32_t bounce_cap, BounceLoop& L,

@@ -47,7 +47,7 @@ void launch_materials_multi_medium(const DevScene& S, const PathState& P, const 
 // The tail of a wave: every remaining bounce of the paths queued in Q.in,
 // one thread per path (k_tail in pt_shade.cuh), at most `cap` bounces in
 // the wave counting the `done` (or *done_ptr) already run; the most bounces
-// a path ran goes to *tail_bounces (atomicMax). Not for radiance-cache waves.
+// a path ran goes to *tail_bounces (atomicMax).
 void launch_tail(const DevScene& S, const PathState& P, const QueueSet& Q, uint32_t max_items,
                  const uint32_t* done_ptr, uint32_t done, uint32_t cap, uint32_t* tail_bounces, cudaStream_t st);
 void launch_tail_plain(const DevScene& S, const PathState& P, const QueueSet& Q, uint32_t max_items,
@@ -56,6 +56,9 @@ void launch_tail_plain(const DevScene& S, const PathState& P, const QueueSet& Q,
 void launch_tail_medium(const DevScene& S, const PathState& P, const QueueSet& Q, uint32_t max_items,
                         const uint32_t* done_ptr, uint32_t done, uint32_t cap, uint32_t* tail_bounces, bool tr, bool tex,
                         cudaStream_t st);
+void launch_tail_cache(const DevScene& S, const PathState& P, const QueueSet& Q, uint32_t max_items,
+                       const uint32_t* done_ptr, uint32_t done, uint32_t cap, uint32_t* tail_bounces, bool tr, bool tex,
+                       cudaStream_t st);
 void launch_tail_multi(const DevScene& S, const PathState& P, const QueueSet& Q, uint32_t max_items,
                        const uint32_t* done_ptr, uint32_t done, uint32_t cap, uint32_t* tail_bounces, bool tr, bool tex,
                        cudaStream_t st);

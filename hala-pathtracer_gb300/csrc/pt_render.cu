@@ -289,6 +289,7 @@ void launch_tail(const DevScene& S, const PathState& P, const QueueSet& Q, uint3
     else launch_tail_multi(S, P, Q, max_items, done_ptr, done, cap, tail_bounces, tr, tex, st);
   } else {
     if (med) launch_tail_medium(S, P, Q, max_items, done_ptr, done, cap, tail_bounces, tr, tex, st);
+    else if (P.c_rec != nullptr) launch_tail_cache(S, P, Q, max_items, done_ptr, done, cap, tail_bounces, tr, tex, st);
     else launch_tail_plain(S, P, Q, max_items, done_ptr, done, cap, tail_bounces, tr, tex, st);
   }
 }

@@ -804,10 +804,10 @@ __global__ void __launch_bounds__(256, MEDIUM ? 4 : 3) k_shade(const __grid_cons
 // the wavefront's; only the schedule differs.
 constexpr uint32_t TAIL_BLOCK = 64;  // small blocks spread the few paths over many SMs
 
-template <int MAT, bool MEDIUM, bool TRANSPARENT, bool MULTI, bool TEXTURED>
+template <int MAT, bool MEDIUM, bool TRANSPARENT, bool MULTI, bool TEXTURED, bool CACHE>
 __device__ __noinline__ ShadeResult tail_shade(const DevScene& S0, const PathState& P, uint32_t p,
                                                unsigned long long& nshadow) {
-  return shade_path<MAT, MEDIUM, TRANSPARENT, MULTI, false, TEXTURED>(S0, P, p, nshadow);
+  return shade_path<MAT, MEDIUM, TRANSPARENT, MULTI, CACHE, TEXTURED>(S0, P, p, nshadow);
 }
 
 // Paths queued in Q.in run at most `cap - done` more bounces, `done` being
@@ -815,7 +815,7 @@ __device__ __noinline__ ShadeResult tail_shade(const DevScene& S0, const PathSta
 // path still alive after that is appended to Q.next (the bounce cap was
 // reached). The most bounces any path ran goes to *tail_bounces (atomicMax),
 // the rays to Q.rays[0] / Q.rays[1].
-template <bool MEDIUM, bool TRANSPARENT, bool MULTI, bool TEXTURED>
+template <bool MEDIUM, bool TRANSPARENT, bool MULTI, bool TEXTURED, bool CACHE>
 __global__ void __launch_bounds__(TAIL_BLOCK) k_tail(const __grid_constant__ DevScene S0, PathState P, QueueSet Q,
                                                      const uint32_t* done_ptr, uint32_t done, uint32_t cap,
                                                      uint32_t* tail_bounces) {
@@ -839,11 +839,11 @@ __global__ void __launch_bounds__(TAIL_BLOCK) k_tail(const __grid_constant__ Dev
       } else {
         ShadeResult r;
         if (cls == MAT_CLASS_DIFFUSE)
-          r = tail_shade<PT_MATERIAL_DIFFUSE, MEDIUM, TRANSPARENT, MULTI, TEXTURED>(S0, P, p, nshadow);
+          r = tail_shade<PT_MATERIAL_DIFFUSE, MEDIUM, TRANSPARENT, MULTI, TEXTURED, CACHE>(S0, P, p, nshadow);
         else if (cls == MAT_CLASS_DISNEY)
-          r = tail_shade<PT_MATERIAL_DISNEY, MEDIUM, TRANSPARENT, MULTI, TEXTURED>(S0, P, p, nshadow);
+          r = tail_shade<PT_MATERIAL_DISNEY, MEDIUM, TRANSPARENT, MULTI, TEXTURED, CACHE>(S0, P, p, nshadow);
         else
-          r = tail_shade<SHADE_DISNEY_GLASS, MEDIUM, TRANSPARENT, MULTI, TEXTURED>(S0, P, p, nshadow);
+          r = tail_shade<SHADE_DISNEY_GLASS, MEDIUM, TRANSPARENT, MULTI, TEXTURED, CACHE>(S0, P, p, nshadow);
         if (r.deferred) nshadow += shadow_path<false, MULTI>(S0, P, p);
         live = !r.stop;
       }
@@ -858,17 +858,17 @@ __global__ void __launch_bounds__(TAIL_BLOCK) k_tail(const __grid_constant__ Dev
   if ((int)lane_id() == __ffs(active) - 1 && most) atomicMax(tail_bounces, most);
 }
 
-template <bool MED, bool MULTI>
+template <bool MED, bool MULTI, bool CACHE = false>
 inline void launch_tail_permutation(const DevScene& S, const PathState& P, const QueueSet& Q, uint32_t max_items,
                                     const uint32_t* done_ptr, uint32_t done, uint32_t cap, uint32_t* tail_bounces,
                                     bool tr, bool tex, cudaStream_t st) {
   const int g = (int)std::max<uint32_t>(1u, (max_items + TAIL_BLOCK - 1) / TAIL_BLOCK);
   if (tr) {
-    if (tex) k_tail<MED, true, MULTI, true><<<g, TAIL_BLOCK, 0, st>>>(S, P, Q, done_ptr, done, cap, tail_bounces);
-    else k_tail<MED, true, MULTI, false><<<g, TAIL_BLOCK, 0, st>>>(S, P, Q, done_ptr, done, cap, tail_bounces);
+    if (tex) k_tail<MED, true, MULTI, true, CACHE><<<g, TAIL_BLOCK, 0, st>>>(S, P, Q, done_ptr, done, cap, tail_bounces);
+    else k_tail<MED, true, MULTI, false, CACHE><<<g, TAIL_BLOCK, 0, st>>>(S, P, Q, done_ptr, done, cap, tail_bounces);
   } else {
-    if (tex) k_tail<MED, false, MULTI, true><<<g, TAIL_BLOCK, 0, st>>>(S, P, Q, done_ptr, done, cap, tail_bounces);
-    else k_tail<MED, false, MULTI, false><<<g, TAIL_BLOCK, 0, st>>>(S, P, Q, done_ptr, done, cap, tail_bounces);
+    if (tex) k_tail<MED, false, MULTI, true, CACHE><<<g, TAIL_BLOCK, 0, st>>>(S, P, Q, done_ptr, done, cap, tail_bounces);
+    else k_tail<MED, false, MULTI, false, CACHE><<<g, TAIL_BLOCK, 0, st>>>(S, P, Q, done_ptr, done, cap, tail_bounces);
   }
 }
 

@@ -340,8 +340,10 @@ pt_status pt_renderer_set_bvh_build(pt_renderer* r, uint32_t mode);
  * default is 16384. The bounce graph switches at its grid sizes (4096 x 4^k
  * paths), so the threshold in effect there is the largest such size not
  * above `paths`. Images, ray counts and bounce counts are the same either
- * way. Radiance-cache renders and the PT_PROFILE_TRACE_TIMING /
- * PT_PROFILE_COUNT instrumentation always use the per-bounce launches. */
+ * way (with a radiance cache attached, the cache's training samples are
+ * gathered in another order, so its images agree to within its training
+ * noise). The PT_PROFILE_TRACE_TIMING / PT_PROFILE_COUNT instrumentation
+ * always uses the per-bounce launches. */
 pt_status pt_renderer_set_tail_paths(pt_renderer* r, uint32_t paths);
 
 /* Traversal limits of this renderer: stack entries per ray (1..96; 0 = 96)
