@@ -948,12 +948,12 @@ __device__ __forceinline__ float bin_child_area(const float4* bin, int32_t node,
   return box_area(a.x, a.z, lz, a.y, a.w, hz);
 }
 
-__global__ void k_collapse(const float4* bin, const CollapseWork* work, uint32_t nwork, float4* out4,
-                           uint32_t* node_counter, uint32_t cap4, CollapseWork* next, uint32_t* next_count,
-                           uint32_t* overflow, uint32_t* leaves) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nwork) return;
-  const CollapseWork w = work[i];
+// One 4-wide node: binary node w.bin's children, opening the largest-area
+// internal child until there are four; internal children are queued for the
+// next level.
+__device__ __forceinline__ void collapse_one(const float4* bin, const CollapseWork w, float4* out4,
+                                             uint32_t* node_counter, uint32_t cap4, CollapseWork* next,
+                                             uint32_t* next_count, uint32_t* overflow, uint32_t* leaves) {
   float lo[4][3], hi[4][3], area[4];
   int32_t link[4];
   int n = 0;
@@ -1019,6 +1019,14 @@ __global__ void k_collapse(const float4* bin, const CollapseWork* work, uint32_t
   for (int c = 0; c < 6; ++c) o[c] = make_float4(q[c][0], q[c][1], q[c][2], q[c][3]);
   o[6] = make_float4(__int_as_float(ol[0]), __int_as_float(ol[1]), __int_as_float(ol[2]), __int_as_float(ol[3]));
   o[7] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+__global__ void k_collapse(const float4* bin, const CollapseWork* work, const uint32_t* work_count, float4* out4,
+                           uint32_t* node_counter, uint32_t cap4, CollapseWork* next, uint32_t* next_count,
+                           uint32_t* overflow, uint32_t* leaves) {
+  const uint32_t nwork = *work_count;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nwork; i += gridDim.x * blockDim.x)
+    collapse_one(bin, work[i], out4, node_counter, cap4, next, next_count, overflow, leaves);
 }
 
 template <class T>
@@ -1152,24 +1160,30 @@ int collapse_bvh4(const float4* bin, uint32_t nn_bin, float4* out4, uint32_t cap
   const uint32_t qcap = nn_bin + 1;
   if (qa.alloc(qcap, st) || qb.alloc(qcap, st) || counters.alloc(5, st)) return 2;
   CollapseWork root{0, 0};
-  uint32_t init[5] = {1, 0, 0, 0, 0};
+  uint32_t init[5] = {1, 1, 0, 0, 0};
   cudaMemcpyAsync(qa.p, &root, sizeof(root), cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(counters.p, init, sizeof(init), cudaMemcpyHostToDevice, st);
-  uint32_t nwork = 1, host = 0;
+  // Levels run in batches without a host round trip: each launch reads its
+  // work count from the level before (a level past the last one finds none),
+  // and the host looks at the count once per batch.
+  const int grid = std::max(1, std::min<int>((int)((qcap + 255) / 256), device_sm_count() * 8));
   CollapseWork* cur = qa.p;
   CollapseWork* nxt = qb.p;
-  int slot = 1;
-  for (int level = 0; level < 200 && nwork > 0; ++level) {
-    cudaMemsetAsync(counters.p + slot, 0, sizeof(uint32_t), st);
-    k_collapse<<<(nwork + 255) / 256, 256, 0, st>>>(bin, cur, nwork, out4, counters.p, cap4, nxt, counters.p + slot,
-                                                   counters.p + 3, counters.p + 4);
-    cudaMemcpyAsync(&host, counters.p + slot, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+  uint32_t* cnt_cur = counters.p + 1;
+  uint32_t* cnt_nxt = counters.p + 2;
+  uint32_t host = 1;
+  for (int level = 0; host > 0;) {
+    if (level >= 256) return 4;
+    for (int k = 0; k < 8; ++k, ++level) {
+      cudaMemsetAsync(cnt_nxt, 0, sizeof(uint32_t), st);
+      k_collapse<<<grid, 256, 0, st>>>(bin, cur, cnt_cur, out4, counters.p, cap4, nxt, cnt_nxt, counters.p + 3,
+                                       counters.p + 4);
+      std::swap(cur, nxt);
+      std::swap(cnt_cur, cnt_nxt);
+    }
+    cudaMemcpyAsync(&host, cnt_cur, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return 3;
-    nwork = host;
-    std::swap(cur, nxt);
-    slot = slot == 1 ? 2 : 1;
   }
-  if (nwork != 0) return 4;
   uint32_t res[5];
   cudaMemcpyAsync(res, counters.p, sizeof(res), cudaMemcpyDeviceToHost, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return 3;

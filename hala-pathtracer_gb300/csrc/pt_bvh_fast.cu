@@ -30,6 +30,7 @@
 // only the traversal work differs.
 #include <cuda_runtime.h>
 
+#include <cuda/atomic>
 #include <cstdint>
 #include <utility>
 
@@ -351,12 +352,13 @@ __global__ void k_fast_bounds(const float4* tlo, const float4* thi, const uint32
                                       fminf(clo[0][2], clo[1][2]), 0.0f));
     __stcg(&boxes[2 * i + 1], make_float4(fmaxf(chi[0][0], chi[1][0]), fmaxf(chi[0][1], chi[1][1]),
                                           fmaxf(chi[0][2], chi[1][2]), 0.0f));
-    __threadfence();
     const int p = i == 0 ? -1 : parent[i];
     if (p < 0) return;
-    const uint32_t before = atomicAdd(&arrived[p], 1u);
+    // release: this node's box is visible to whoever continues at p;
+    // acquire: if that is this thread, it sees the other child's box
+    cuda::atomic_ref<uint32_t, cuda::thread_scope_device> arrivals(arrived[p]);
+    const uint32_t before = arrivals.fetch_add(1u, cuda::std::memory_order_acq_rel);
     if (before + 1u < needed[p]) return;  // the other child is not finished: its thread continues
-    __threadfence();
     i = p;
   }
 }

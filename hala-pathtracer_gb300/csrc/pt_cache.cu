@@ -800,7 +800,7 @@ void pt_cache_config_default(pt_cache_config* c) {
   if (!c) return;
   std::memset(c, 0, sizeof(*c));
   c->query_depth = 1;
-  c->train_shift = 4;
+  c->train_shift = 5;
   c->weight_grad_kernel = 0;
   c->batch_size = 1u << 16;
   c->log2_table_size = 19;
@@ -809,7 +809,7 @@ void pt_cache_config_default(pt_cache_config* c) {
   c->max_resolution = 2048;
   c->seed = 1;
   c->warmup_frames = 1;
-  c->paths_per_pass = 1u << 20;
+  c->paths_per_pass = 1u << 21;
   c->steps_per_pass = 1;
 }
 

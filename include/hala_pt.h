@@ -545,7 +545,7 @@ typedef struct pt_cache pt_cache;
 
 struct pt_cache_config {
   uint32_t query_depth;     /* vertex index at which paths end in the cache (1 = first bounce) */
-  uint32_t train_shift;     /* 1 in 2^train_shift paths trains the cache (4 = 1/16) */
+  uint32_t train_shift;     /* 1 in 2^train_shift paths trains the cache (5 = 1/32) */
   uint32_t batch_size;      /* training batch in samples (multiple of 16) */
   uint32_t log2_table_size; /* hash-table entries per level = 2^log2_table_size */
   float learning_rate;      /* Adam learning rate */
@@ -562,8 +562,8 @@ struct pt_cache_config {
                                   kernel (kept for comparison) */
 };
 
-/* query_depth 1, 1/16 training paths, batch 65536, 2^19 entries, lr 1e-2,
- * resolutions 16..2048, seed 1, one warm-up frame, passes of 2^20 paths,
+/* query_depth 1, 1/32 training paths, batch 65536, 2^19 entries, lr 1e-2,
+ * resolutions 16..2048, seed 1, one warm-up frame, passes of 2^21 paths,
  * at least one optimiser step per pass, tcgen05 weight gradients. */
 void pt_cache_config_default(pt_cache_config* config);
 pt_status pt_cache_create(const pt_cache_config* config, pt_cache** out);
