@@ -83,12 +83,28 @@ __device__ __forceinline__ void init_path(const DevScene& S, const PathState& P,
   if (P.c_train) P.c_train[i] = 0xFFFFFFFFu;
 }
 
+// Queue position of path slot i: slots are read as rows of `width` (slot
+// i + width is the pixel below slot i), and each band of 4 rows is queued
+// tile by tile, 8 x 4 pixels per tile, so that the 32 paths of a warp start
+// from a compact patch of the image instead of a 32-pixel strip. A bijection
+// on [0, n): slots past the last whole band, and widths that are not a
+// multiple of 8, keep their own position. Only the order in which the
+// kernels visit paths changes, not any path's result.
+__device__ __forceinline__ uint32_t tiled_position(uint32_t i, uint32_t n, uint32_t width) {
+  if (width % 8u != 0u) return i;
+  const uint64_t band = 4ull * width;
+  const uint64_t b = i / band;
+  if ((b + 1) * band > n) return i;
+  const uint32_t r = (uint32_t)(i - b * band), ly = r / width, col = r % width;
+  return (uint32_t)(b * band) + (col >> 3) * 32u + ly * 8u + (col & 7u);
+}
+
 __global__ void k_camera(const __grid_constant__ DevScene S, PathState P, uint64_t g0, uint32_t n,
                          uint32_t* q_active, uint32_t* active_count) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   init_path(S, P, i, g0 + i);
-  q_active[i] = i;
+  q_active[tiled_position(i, n, S.width)] = i;
   if (i == 0) *active_count = n;
 }
 
