@@ -276,8 +276,8 @@ uint64_t renderer_estimate_bytes(const pt_scene_desc* d, uint32_t width, uint32_
   }
   const uint64_t V = std::max<uint64_t>(nv, 1), T = std::max<uint64_t>(nt, 1);
   // vertices: raw 44 + normal/tangent/position 48 + uv 8
-  // triangles: raw indices 12 + v0/e1/e2 48 + sorted 48 + 4-wide nodes
-  // (capacity 2 per triangle) 256 + vertex ids 12 + material 4 + shading
+  // triangles: raw indices 12 + v0/e1/e2 48 + sorted 48 + wide nodes
+  // (capacity one per triangle, at most 256 B each) 256 + vertex ids 12 + material 4 + shading
   // record 96; the BVH build's scratch (binary nodes and queues) is about
   // 190 B more
   uint64_t b = V * 100 + T * (476 + 190);
@@ -844,7 +844,7 @@ pt_status pt_renderer_commit(pt_renderer* r) {
   CK(r, r->tri_sorted.ensure(3 * (size_t)std::max<uint32_t>(r->ntris, 1)));
   CK(r, cudaEventRecord(r->ev0, st));
   if (r->ntris > 0) {
-    // binary SAH tree first (scratch), then its 4-wide collapse for traversal
+    // binary SAH tree first (scratch), then its wide collapse for traversal
     Buf<float4> bin;
     const uint32_t cap = 2 * r->ntris;
     CK(r, bin.ensure(4 * (size_t)cap));
@@ -854,16 +854,19 @@ pt_status pt_renderer_commit(pt_renderer* r) {
                                                : build_bvh(r->tri_v0.p, r->tri_e1.p, r->tri_e2.p, r->ntris, bb, &nn, st);
     if (rc == 2) return fail(r, PT_ERR_OOM, "BVH build: out of device memory");
     if (rc != 0) return fail(r, PT_ERR_CUDA, "BVH build failed (code " + std::to_string(rc) + ")");
-    CK(r, r->nodes.ensure(8 * (size_t)std::max<uint32_t>(nn, 1)));
+    // every wide node starts from a distinct internal binary node, and a
+    // binary tree of nn nodes has fewer than nn / 2 + 1 of them
+    const uint32_t cap_wide = nn / 2 + 1;
+    CK(r, r->nodes.ensure(NODE_F4 * (size_t)cap_wide));
     uint32_t leaves = 0;
-    rc = collapse_bvh4(bin.p, nn, r->nodes.p, std::max<uint32_t>(nn, 1), &nn4, st, &leaves);
+    rc = collapse_wide(bin.p, nn, r->nodes.p, cap_wide, &nn4, st, &leaves);
     if (rc == 2) return fail(r, PT_ERR_OOM, "BVH collapse: out of device memory");
     if (rc != 0) return fail(r, PT_ERR_CUDA, "BVH collapse failed (code " + std::to_string(rc) + ")");
     r->nnodes = nn4;
     r->stats.bvh_binary_nodes = 2ull * leaves - 1;  // reachable from the root (the build reserves more slots)
   } else {
     r->stats.bvh_binary_nodes = 0;
-    CK(r, r->nodes.ensure(8));
+    CK(r, r->nodes.ensure(NODE_F4));
     r->nnodes = 0;
   }
   CK(r, cudaEventRecord(r->ev1, st));

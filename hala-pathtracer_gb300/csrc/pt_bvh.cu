@@ -10,7 +10,7 @@
 // LARGE_TASK triangles (the top levels of big scenes) are spread over many
 // blocks instead (k_large_*), with the same planes and the same partition
 // order. A layout pass then writes the 64-byte binary nodes and the
-// triangles in leaf order; k_collapse turns the binary tree into the 4-wide
+// triangles in leaf order; k_collapse turns the binary tree into the wide
 // traversal nodes.
 #include <cuda.h>  // driver types only (the driver call is reached through cudaGetDriverEntryPointByVersion)
 #include <cuda_runtime.h>
@@ -932,13 +932,14 @@ __global__ void k_reorder(const uint32_t* final_ids, uint32_t n, const float4* v
 // Build scratch from the stream-ordered allocator of the build stream: no
 // allocation or free here waits for work on other streams.
 // ---------------------------------------------------------------------------
-// Collapse of the binary BVH into the 4-wide traversal layout (pt_types.h):
-// each 4-wide node takes a binary node's two children and keeps replacing
+// Collapse of the binary BVH into the wide traversal layout (pt_types.h):
+// each wide node takes a binary node's two children and keeps replacing
 // its internal child of largest surface area by that child's two children
-// until it has four. One launch per level of the 4-wide tree.
+// until it has BVH_WIDTH. One launch per level of the wide tree (the host
+// reads the remaining work once per eight levels).
 struct CollapseWork {
   int32_t bin;  // binary node
-  int32_t out;  // its 4-wide node
+  int32_t out;  // its wide node
 };
 
 __device__ __forceinline__ float bin_child_area(const float4* bin, int32_t node, int c) {
@@ -948,14 +949,14 @@ __device__ __forceinline__ float bin_child_area(const float4* bin, int32_t node,
   return box_area(a.x, a.z, lz, a.y, a.w, hz);
 }
 
-// One 4-wide node: binary node w.bin's children, opening the largest-area
-// internal child until there are four; internal children are queued for the
-// next level.
+// One wide node: binary node w.bin's children, opening the largest-area
+// internal child until there are BVH_WIDTH; internal children are queued
+// for the next level.
 __device__ __forceinline__ void collapse_one(const float4* bin, const CollapseWork w, float4* out4,
                                              uint32_t* node_counter, uint32_t cap4, CollapseWork* next,
                                              uint32_t* next_count, uint32_t* overflow, uint32_t* leaves) {
-  float lo[4][3], hi[4][3], area[4];
-  int32_t link[4];
+  float lo[BVH_WIDTH][3], hi[BVH_WIDTH][3], area[BVH_WIDTH];
+  int32_t link[BVH_WIDTH];
   int n = 0;
   // child c of binary node `node` into slot k
   auto load = [&](int32_t node, int c, int k) {
@@ -974,7 +975,7 @@ __device__ __forceinline__ void collapse_one(const float4* bin, const CollapseWo
   load(w.bin, 0, 0);
   load(w.bin, 1, 1);
   n = 2;
-  while (n < 4) {
+  while (n < BVH_WIDTH) {
     int best = -1;
     float ba = -1.0f;
     for (int k = 0; k < n; ++k)
@@ -984,14 +985,14 @@ __device__ __forceinline__ void collapse_one(const float4* bin, const CollapseWo
       }
     if (best < 0) break;
     const int32_t node = link[best];
-    load(node, 1, n);     // second child appended (n < 4 here)
+    load(node, 1, n);     // second child appended (n < BVH_WIDTH here)
     load(node, 0, best);  // first child replaces its parent
     ++n;
   }
-  float4* o = out4 + 8 * (size_t)w.out;
-  float q[6][4];
-  int32_t ol[4];
-  for (int k = 0; k < 4; ++k) {
+  float4* o = out4 + NODE_F4 * (size_t)w.out;
+  float q[6][BVH_WIDTH];
+  int32_t ol[BVH_WIDTH];
+  for (int k = 0; k < BVH_WIDTH; ++k) {
     if (k < n) {
       for (int c = 0; c < 3; ++c) {
         q[2 * c][k] = lo[k][c];
@@ -1016,9 +1017,13 @@ __device__ __forceinline__ void collapse_one(const float4* bin, const CollapseWo
       ol[k] = EMPTY_LINK;
     }
   }
-  for (int c = 0; c < 6; ++c) o[c] = make_float4(q[c][0], q[c][1], q[c][2], q[c][3]);
-  o[6] = make_float4(__int_as_float(ol[0]), __int_as_float(ol[1]), __int_as_float(ol[2]), __int_as_float(ol[3]));
-  o[7] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  for (int g = 0; g < BVH_GROUPS; ++g) {
+    for (int c = 0; c < 6; ++c)
+      o[6 * g + c] = make_float4(q[c][4 * g], q[c][4 * g + 1], q[c][4 * g + 2], q[c][4 * g + 3]);
+    o[6 * BVH_GROUPS + g] = make_float4(__int_as_float(ol[4 * g]), __int_as_float(ol[4 * g + 1]),
+                                        __int_as_float(ol[4 * g + 2]), __int_as_float(ol[4 * g + 3]));
+    o[7 * BVH_GROUPS + g] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  }
 }
 
 __global__ void k_collapse(const float4* bin, const CollapseWork* work, const uint32_t* work_count, float4* out4,
@@ -1152,11 +1157,11 @@ int build_bvh(const float4* tri_v0, const float4* tri_e1, const float4* tri_e2, 
   return 0;
 }
 
-int collapse_bvh4(const float4* bin, uint32_t nn_bin, float4* out4, uint32_t cap4, uint32_t* num4, cudaStream_t st,
+int collapse_wide(const float4* bin, uint32_t nn_bin, float4* out4, uint32_t cap4, uint32_t* num4, cudaStream_t st,
                   uint32_t* num_leaves) {
   if (nn_bin == 0 || cap4 == 0) return 2;
   Tmp<CollapseWork> qa, qb;
-  Tmp<uint32_t> counters;  // [0] 4-wide nodes, [1] next queue A, [2] next queue B, [3] overflow, [4] leaves
+  Tmp<uint32_t> counters;  // [0] wide nodes, [1] next queue A, [2] next queue B, [3] overflow, [4] leaves
   const uint32_t qcap = nn_bin + 1;
   if (qa.alloc(qcap, st) || qb.alloc(qcap, st) || counters.alloc(5, st)) return 2;
   CollapseWork root{0, 0};

@@ -24,7 +24,7 @@
 //      (an atomic counter per node);
 //   6. the triangles in key order.
 // The output is the binary traversal layout of pt_bvh.cu (node 0 the root),
-// which collapse_bvh4 turns into the 4-wide tree. Closest hits do not depend
+// which collapse_wide turns into the wide tree. Closest hits do not depend
 // on the tree (lexicographic minimum of (t, id) over the triangles the
 // conservative boxes admit), so the images are those of the default build;
 // only the traversal work differs.

@@ -113,10 +113,10 @@ int build_bvh(const float4* tri_v0, const float4* tri_e1, const float4* tri_e2, 
 // (fewer passes, no host round trip per level, a tree of lower quality).
 int build_bvh_fast(const float4* tri_v0, const float4* tri_e1, const float4* tri_e2, uint32_t ntris,
                    BvhBuffers& out, uint32_t* num_nodes, cudaStream_t st);
-// Collapses the binary tree (64-B nodes) into 4-wide nodes (8 float4 each,
-// at most cap4 of them); *num_leaves (optional) receives the tree's leaf
-// count. Returns 0 on success.
-int collapse_bvh4(const float4* bin, uint32_t nn_bin, float4* out4, uint32_t cap4, uint32_t* num4, cudaStream_t st,
+// Collapses the binary tree (64-B nodes) into BVH_WIDTH-wide nodes (NODE_F4
+// float4 each, at most cap4 of them); *num_leaves (optional) receives the
+// tree's leaf count. Returns 0 on success.
+int collapse_wide(const float4* bin, uint32_t nn_bin, float4* out4, uint32_t cap4, uint32_t* num4, cudaStream_t st,
                   uint32_t* num_leaves = nullptr);
 
 }  // namespace hpt

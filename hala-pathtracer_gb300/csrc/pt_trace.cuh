@@ -152,7 +152,7 @@ __device__ __forceinline__ SlabRay slab_ray(float3 o, float3 d) {
 // the best is skipped. The oracle's BVH uses the same slack.
 constexpr float TRAV_T_SLACK = 1.0f + 1.0f / 4096.0f;
 
-// Slab test of the four children of a 4-wide node, one lane per child. The
+// Slab test of four children of a wide node (one group of four). The
 // near and far planes of each axis are picked by the ray's direction signs
 // when loading, which gives exactly min/max of the two plane distances (the
 // distance is monotonic in the plane coordinate, lo <= hi). The slab interval
@@ -190,7 +190,23 @@ __device__ __forceinline__ void cswap(float& ka, int32_t& va, float& kb, int32_t
   }
 }
 
-constexpr int TRAV4_STACK = 96;  // up to three entries per level of the 4-wide tree
+// Ascending sort of a node's (entry distance, link) pairs: the optimal
+// networks of 5 (four children) and 19 (eight children) comparators.
+__device__ __forceinline__ void sort_children(float (&k)[4], int32_t (&v)[4]) {
+  cswap(k[0], v[0], k[1], v[1]);
+  cswap(k[2], v[2], k[3], v[3]);
+  cswap(k[0], v[0], k[2], v[2]);
+  cswap(k[1], v[1], k[3], v[3]);
+  cswap(k[1], v[1], k[2], v[2]);
+}
+__device__ __forceinline__ void sort_children(float (&k)[8], int32_t (&v)[8]) {
+  constexpr int net[19][2] = {{0, 2}, {1, 3}, {4, 6}, {5, 7}, {0, 4}, {1, 5}, {2, 6}, {3, 7}, {0, 1}, {2, 3},
+                              {4, 5}, {6, 7}, {2, 4}, {3, 5}, {1, 4}, {3, 6}, {1, 2}, {3, 4}, {5, 6}};
+#pragma unroll
+  for (int c = 0; c < 19; ++c) cswap(k[net[c][0]], v[net[c][0]], k[net[c][1]], v[net[c][1]]);
+}
+
+constexpr int TRAV4_STACK = 96;  // up to BVH_WIDTH - 1 entries per level of the wide tree
 // Upper bound on node visits of one traversal; a well-formed tree never
 // reaches it, a corrupt one ends the traversal instead of looping.
 constexpr uint32_t TRAV_MAX_VISITS = 1u << 22;
@@ -242,21 +258,27 @@ __device__ __forceinline__ HitRec trace_tris_closest(const DevScene& S, float3 o
         return h;
       }
       if (COUNT) tc->nodes++;
-      const float4* nd = S.nodes + 8 * (size_t)cur;
-      float tn[4];
-      bool hit[4];
-      quad_slabs(nd, sr, tmin, h.t, tn, hit);
-      const int4 l = __ldg(reinterpret_cast<const int4*>(nd + 6));
+      const float4* nd = S.nodes + NODE_F4 * (size_t)cur;
       // nearest first: sort (distance, link) with misses at +inf
-      float k0 = hit[0] ? tn[0] : INF, k1 = hit[1] ? tn[1] : INF, k2 = hit[2] ? tn[2] : INF,
-            k3 = hit[3] ? tn[3] : INF;
-      int32_t v0 = l.x, v1 = l.y, v2 = l.z, v3 = l.w;
-      const int nh = (int)hit[0] + (int)hit[1] + (int)hit[2] + (int)hit[3];
-      cswap(k0, v0, k1, v1);
-      cswap(k2, v2, k3, v3);
-      cswap(k0, v0, k2, v2);
-      cswap(k1, v1, k3, v3);
-      cswap(k1, v1, k2, v2);
+      float k[BVH_WIDTH];
+      int32_t v[BVH_WIDTH];
+      int nh = 0;
+#pragma unroll
+      for (int g = 0; g < BVH_GROUPS; ++g) {
+        float tn[4];
+        bool hit[4];
+        quad_slabs(nd + 6 * g, sr, tmin, h.t, tn, hit);
+        const int4 l = __ldg(reinterpret_cast<const int4*>(nd + 6 * BVH_GROUPS + g));
+        const int32_t L[4] = {l.x, l.y, l.z, l.w};
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          k[4 * g + c] = hit[c] ? tn[c] : INF;
+          v[4 * g + c] = L[c];
+          nh += (int)hit[c];
+        }
+      }
+      sort_children(k, v);
+      const int32_t v0 = v[0];
       if (nh == 0) {
         cur = 0x7FFFFFFF;
         while (sp > 0) {
@@ -270,9 +292,13 @@ __device__ __forceinline__ HitRec trace_tris_closest(const DevScene& S, float3 o
         continue;
       }
       if (sp + nh - 1 > lim) trav_error(S, TRAV_ERR_STACK);  // a far child is dropped below
-      if (nh >= 4 && sp < lim) { st_link[sp] = v3; st_t[sp] = k3; ++sp; }
-      if (nh >= 3 && sp < lim) { st_link[sp] = v2; st_t[sp] = k2; ++sp; }
-      if (nh >= 2 && sp < lim) { st_link[sp] = v1; st_t[sp] = k1; ++sp; }
+#pragma unroll
+      for (int j = BVH_WIDTH - 1; j >= 1; --j)
+        if (nh > j && sp < lim) {
+          st_link[sp] = v[j];
+          st_t[sp] = k[j];
+          ++sp;
+        }
       cur = v0;
     }
     // leaf
@@ -322,19 +348,22 @@ __device__ __forceinline__ bool trace_tris_any(const DevScene& S, float3 o, floa
         trav_error(S, TRAV_ERR_VISITS);
         return false;
       }
-      const float4* nd = S.nodes + 8 * (size_t)cur;
-      float tn[4];
-      bool hit[4];
-      quad_slabs(nd, sr, tmin, tmax, tn, hit);
-      const int4 l = __ldg(reinterpret_cast<const int4*>(nd + 6));
-      const int32_t L[4] = {l.x, l.y, l.z, l.w};
+      const float4* nd = S.nodes + NODE_F4 * (size_t)cur;
       int32_t next = 0x7FFFFFFF;
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        if (!hit[k]) continue;
-        if (next == 0x7FFFFFFF) next = L[k];
-        else if (sp < lim) stack[sp++] = L[k];
-        else trav_error(S, TRAV_ERR_STACK);
+      for (int g = 0; g < BVH_GROUPS; ++g) {
+        float tn[4];
+        bool hit[4];
+        quad_slabs(nd + 6 * g, sr, tmin, tmax, tn, hit);
+        const int4 l = __ldg(reinterpret_cast<const int4*>(nd + 6 * BVH_GROUPS + g));
+        const int32_t L[4] = {l.x, l.y, l.z, l.w};
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          if (!hit[c]) continue;
+          if (next == 0x7FFFFFFF) next = L[c];
+          else if (sp < lim) stack[sp++] = L[c];
+          else trav_error(S, TRAV_ERR_STACK);
+        }
       }
       if (next == 0x7FFFFFFF) {
         if (sp == 0) return false;

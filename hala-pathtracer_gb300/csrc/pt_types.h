@@ -18,6 +18,15 @@
 //   wave     SoA path state sized for `wave_paths` paths (see PathState)
 //   images   accum/albedo/normal float4 per pixel, final uchar4 per pixel
 #pragma once
+
+// Children per traversal node, 4 or 8 (compile time). Measured on the GB300
+// (Disney grid): 8-wide nodes cut node visits per ray from 10.2 to 6.8 but
+// made each visit dearer (two slab groups, a 19-comparator sort, spills at
+// the traversal kernels' register cap): closest hit 6.07 -> 7.90 ms per
+// launch. 4 is the default.
+#ifndef HPT_BVH_WIDTH
+#define HPT_BVH_WIDTH 4
+#endif
 #include <cstdint>
 
 #include "../../include/hala_pt.h"
@@ -52,14 +61,22 @@ struct DevCamera {  // inc/types.glsl:2-11
 // link >= 0: internal node index; link < 0: leaf, start = link & 0x03FFFFFF
 // (slot in tri[]), count = (link >> 26) & 0x1F. An empty child has an
 // inverted box so it never intersects.
-// 4-wide BVH node used by the traversal (128 B = 8 x 16 B):
-//   q[0..5] = lo.x, hi.x, lo.y, hi.y, lo.z, hi.z of the four children
-//   q[6]    = the four child links (as above; EMPTY_LINK for an unused slot,
-//             whose box is +inf on every bound so that no ray enters it:
-//             both slab distances of an axis are then +inf or -inf)
-//   q[7]    = unused
-// It is collapsed from the binary tree: halving the depth halves the chain
-// of dependent node fetches a ray waits on.
+// Wide BVH node used by the traversal: BVH_WIDTH children in groups of 4,
+// NODE_F4 16-byte words (32 B per child):
+//   q[6g .. 6g+5]     = lo.x, hi.x, lo.y, hi.y, lo.z, hi.z of the four
+//                       children of group g
+//   q[6G + g]         = the four child links of group g (as above;
+//                       EMPTY_LINK for an unused slot, whose box is +inf on
+//                       every bound so that no ray enters it: both slab
+//                       distances of an axis are then +inf or -inf)
+//   q[7G .. 8G - 1]   = unused
+// with G = BVH_WIDTH / 4 groups. It is collapsed from the binary tree:
+// a node of width W replaces log2(W) binary levels, which shortens the
+// chain of dependent node fetches a ray waits on.
+constexpr int BVH_WIDTH = HPT_BVH_WIDTH;
+constexpr int BVH_GROUPS = BVH_WIDTH / 4;
+constexpr int NODE_F4 = 8 * BVH_GROUPS;
+static_assert(BVH_WIDTH == 4 || BVH_WIDTH == 8, "4- or 8-wide nodes");
 constexpr int32_t EMPTY_LINK = 0x7FFFFFFF;
 constexpr int32_t LEAF_BIT = (int32_t)0x80000000u;
 constexpr int LEAF_MAX = 8;
