@@ -52,6 +52,8 @@ cudaError_t WaveBuffers::ensure(uint32_t want, bool want_med, bool want_multi) {
   if (want_med) {
     chk(med0.ensure(want));
     chk(med1.ensure(want));
+    chk(sh_f0.ensure(want));
+    chk(sh_f1.ensure(want));
   }
   if (want_multi) chk(job.ensure(want));
   chk(sh_o.ensure(want));
@@ -85,6 +87,8 @@ cudaError_t WaveBuffers::ensure(uint32_t want, bool want_med, bool want_multi) {
   P.normal = normal.p;
   P.med0 = med ? med0.p : nullptr;
   P.med1 = med ? med1.p : nullptr;
+  P.sh_f0 = med ? sh_f0.p : nullptr;
+  P.sh_f1 = med ? sh_f1.p : nullptr;
   P.sh_o = sh_o.p;
   P.sh_d0 = sh_d0.p;
   P.sh_d1 = sh_d1.p;
@@ -100,7 +104,7 @@ void WaveBuffers::release() {
   Buf<uint4>* b4[] = {&rng};
   for (auto* b : b4) b->release();
   Buf<float4>* f4[] = {&ray_o, &ray_d, &hit, &thr, &rad, &albedo, &normal, &med0,
-                       &sh_o, &sh_d0, &sh_d1, &sh_c0, &sh_c1, &sh_T};
+                       &sh_o, &sh_d0, &sh_d1, &sh_c0, &sh_c1, &sh_T, &sh_f0, &sh_f1};
   for (auto* b : f4) b->release();
   med1.release();
   Buf<uint32_t>* u[] = {&depth, &flags, &job, &q_a, &q_b, &q_logic, &q_diff, &q_dis, &q_glass, &q_shadow, &counters};
@@ -113,8 +117,9 @@ void WaveBuffers::release() {
 
 uint64_t WaveBuffers::bytes_per_path(bool med, bool multi) {
   // rng 16, ray_o/ray_d/hit/thr/rad/albedo/normal 7x16, depth+flags 8,
-  // six NEE float4 96, seven queues 28 (+ medium 24, + job slot 4)
-  return 16 + 7 * 16 + 8 + 96 + 28 + (med ? 24 : 0) + (multi ? 4 : 0);
+  // six NEE float4 96, seven queues 28 (+ medium 24 and two NEE float4 32,
+  // + job slot 4)
+  return 16 + 7 * 16 + 8 + 96 + 28 + (med ? 56 : 0) + (multi ? 4 : 0);
 }
 
 cudaError_t run_bounces(const DevScene& S, WaveBuffers& W, uint32_t live, uint32_t max_depth, BounceLoop& L,
@@ -122,7 +127,10 @@ cudaError_t run_bounces(const DevScene& S, WaveBuffers& W, uint32_t live, uint32
   uint32_t* cnt0 = W.counters.p;
   uint32_t* cnt1 = W.counters.p + Q_COUNT;
   const uint32_t bounce_cap = 4u * max_depth + 4096u;
-  const uint64_t per_bounce = (S.features & PT_FEATURE_MEDIUM) ? 5 : 6;  // trace, logic, 3 shades (, shadow)
+  // trace, logic, 3 shades, and shadow rays (k_shadow, or k_transmit with
+  // media unless a material is transparent)
+  const bool med_tr = (S.features & PT_FEATURE_MEDIUM) && (S.features & PT_FEATURE_TRANSPARENT);
+  const uint64_t per_bounce = med_tr ? 5 : 6;
   if (live == 0) {
     L.bounces = 0;
     L.timed_out = false;

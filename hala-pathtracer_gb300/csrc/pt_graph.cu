@@ -252,7 +252,8 @@ cudaError_t run_bounces_graph(const DevScene& S, WaveBuffers& W, uint32_t bounce
     return e;
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
   const uint32_t done = pinned[G_DONE], live = pinned[G_LIVE], tail_bounces = pinned[G_TAIL];
-  const uint64_t per_bounce = (S.features & PT_FEATURE_MEDIUM) ? 5 : 6;
+  const bool med_tr = (S.features & PT_FEATURE_MEDIUM) && (S.features & PT_FEATURE_TRANSPARENT);
+  const uint64_t per_bounce = med_tr ? 5 : 6;
   const uint64_t cases = done - tail_bounces + (tail_bounces ? 1 : 0);  // switch cases that ran
   L.bounces = done;
   L.timed_out = live > 0;

@@ -158,6 +158,16 @@ __global__ void __launch_bounds__(256, 5) k_shadow(const __grid_constant__ DevSc
     count_add(&Q.rays[1], shadow_path<BRUTE, MULTI>(S0, P, Q.shadow[i]));
 }
 
+// Next-event rays of vertices with media when no material is transparent
+// (inc/lighting.glsl:7-61 and :69-244: transmittance, visibility, then
+// radiance += T * Ld), deferred from the shading kernels like k_shadow's.
+template <bool MULTI>
+__global__ void __launch_bounds__(256, 4) k_transmit(const __grid_constant__ DevScene S0, PathState P, QueueSet Q) {
+  const uint32_t n = Q.counts[Q_SHADOW];
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    count_add(&Q.rays[1], transmit_path<MULTI>(S0, P, Q.shadow[i]));
+}
+
 // ------------------------------------------------------------------ accumulation
 // pathtracer.rgen.glsl:259-278: running mean per pixel in frame order.
 // Global path index g = frame * WH + pixel (frame counted from the last
@@ -286,12 +296,14 @@ void launch_shade(const DevScene& S, const PathState& P, const QueueSet& Q, uint
     if (med) launch_materials_multi_medium(S, P, Q, g, tr, tex, st);
     else launch_materials_multi(S, P, Q, g, tr, tex, st);
     if (!med) k_shadow<false, true><<<g, 256, 0, st>>>(S, P, Q);
+    else if (!tr) k_transmit<true><<<g, 256, 0, st>>>(S, P, Q);
   } else {
     k_shade_logic<false><<<g, 256, 0, st>>>(S, P, Q);
     if (med) launch_materials_medium(S, P, Q, g, tr, tex, st);  // the cache is refused for scenes with media
     else if (P.c_rec != nullptr) launch_materials_cache(S, P, Q, g, tr, tex, st);
     else launch_materials_plain(S, P, Q, g, tr, tex, st);
     if (!med) k_shadow<false, false><<<g, 256, 0, st>>>(S, P, Q);
+    else if (!tr) k_transmit<false><<<g, 256, 0, st>>>(S, P, Q);
   }
 }
 

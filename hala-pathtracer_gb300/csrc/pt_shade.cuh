@@ -315,6 +315,36 @@ __global__ void __launch_bounds__(256) k_shade_logic(const __grid_constant__ Dev
     logic_path<MULTI>(S0, P, Q.logic[i]);
 }
 
+// inc/lighting.glsl:7-61 (MEDIUM && VOL_MIS): transmittance along a shadow
+// ray through refractive (and, with TRANSPARENT, transparent) surfaces and
+// the media behind them. Draws random numbers only with TRANSPARENT; counts
+// its closest-hit rays in `nrays`.
+template <bool TRANSPARENT>
+__device__ __forceinline__ float3 transmittance(const DevScene& S, uint4& rng, float3 o, float3 d,
+                                                unsigned long long& nrays) {
+  float3 T = f3(1.0f);
+  for (uint32_t depth = 0; depth < S.max_depth; ++depth) {
+    ++nrays;
+    HitRec h = trace_closest<false>(S, o, d, 0.0f, WORLD_SIZE);
+    if (h.id == HIT_MISS || (h.id & HIT_LIGHT_BIT)) break;
+    uint32_t mi = __ldg(&S.tri_mat[h.id]);
+    if (mi >= S.num_mats) return f3(0.0f);
+    const pt_material& m = S.mats[mi];
+    bool transparent = false;
+    if (TRANSPARENT) transparent = m.opacity == 0.0f || rand1(rng) > m.opacity;
+    bool refractive = (1.0f - m.metallic) * m.specular_transmission > 0.0f;
+    if (!(transparent || refractive)) return f3(0.0f);
+    float3 nrm = interp_normal(S, h.id, h.u, h.v);
+    if (dot(d, nrm) > 0.0f && m.medium.type != PT_MEDIUM_NONE) {
+      float3 col = m.medium.type == PT_MEDIUM_ABSORB ? f3(1.0f) - f3(m.medium.color) : f3(1.0f);
+      T *= vexp(-col * m.medium.density * h.t);
+    }
+    float3 fhp = o + d * h.t;
+    o = fhp + d * EPS;
+  }
+  return T;
+}
+
 // ------------------------------------------------------------------ surface shading
 template <int MAT>
 struct Shader {
@@ -323,30 +353,9 @@ struct Shader {
   uint32_t hash;
   unsigned long long nshadow;
 
-  // inc/lighting.glsl:7-61 (MEDIUM && VOL_MIS)
   template <bool TRANSPARENT>
   __device__ float3 eval_transmittance(float3 o, float3 d) {
-    float3 T = f3(1.0f);
-    for (uint32_t depth = 0; depth < S.max_depth; ++depth) {
-      ++nshadow;
-      HitRec h = trace_closest<false>(S, o, d, 0.0f, WORLD_SIZE);
-      if (h.id == HIT_MISS || (h.id & HIT_LIGHT_BIT)) break;
-      uint32_t mi = __ldg(&S.tri_mat[h.id]);
-      if (mi >= S.num_mats) return f3(0.0f);
-      const pt_material& m = S.mats[mi];
-      bool transparent = false;
-      if (TRANSPARENT) transparent = m.opacity == 0.0f || rand1(rng) > m.opacity;
-      bool refractive = (1.0f - m.metallic) * m.specular_transmission > 0.0f;
-      if (!(transparent || refractive)) return f3(0.0f);
-      float3 nrm = interp_normal(S, h.id, h.u, h.v);
-      if (dot(d, nrm) > 0.0f && m.medium.type != PT_MEDIUM_NONE) {
-        float3 col = m.medium.type == PT_MEDIUM_ABSORB ? f3(1.0f) - f3(m.medium.color) : f3(1.0f);
-        T *= vexp(-col * m.medium.density * h.t);
-      }
-      float3 fhp = o + d * h.t;
-      o = fhp + d * EPS;
-    }
-    return T;
+    return transmittance<TRANSPARENT>(S, rng, o, d, nshadow);
   }
 
   // inc/lighting.glsl:69-244 with the transmittance evaluated in-thread.
@@ -413,11 +422,88 @@ struct Shader {
     }
     return Ld;
   }
+
+  // direct_lighting_volmis of a scene without transparent materials, whose
+  // transmittance draws no random numbers: the light samples are drawn here
+  // in the same order, and the two shadow rays with the factors of their
+  // contributions are stored for k_transmit, which traces them, mixes the
+  // visibility events into the hash and adds the light as the in-thread
+  // form does. `T` is the throughput the contribution is scaled by. Returns
+  // the pending-ray bits (PEND_ENV, PEND_LIGHT).
+  __device__ uint32_t prepare_volmis(const PathState& P, uint32_t p, const pt_material& mat, bool is_surface,
+                                     bool ans, const SurfState& st, float3 fhp, float3 raydir, float aniso,
+                                     float3 T);
 };
 
 // Pending-event word stored with the shadow rays (applied to the hash after
 // the visibility events, in the reference's order).
 constexpr uint32_t PEND_ENV = 1u, PEND_LIGHT = 2u, PEND_BSDF = 4u, PEND_STOP = 8u, PEND_RR = 16u;
+
+template <int MAT>
+__device__ uint32_t Shader<MAT>::prepare_volmis(const PathState& P, uint32_t p, const pt_material& mat,
+                                                bool is_surface, bool ans, const SurfState& st, float3 fhp,
+                                                float3 raydir, float aniso, float3 T) {
+  uint32_t pend = 0;
+  const float3 scatter_pos = fhp + st.ffnormal * EPS;
+  if (S.env_map) {
+    float3 em;
+    float light_pdf;
+    float3 ldir = sample_env_map(S, rng, em, light_pdf);
+    if (light_pdf > 0.0f) {
+      float pdf = 0.0f;
+      float3 f = f3(0.0f);
+      if (is_surface) {
+        f = bsdf_eval<MAT, false>(st.fr, mat, ans, -raydir, st.ffnormal, ldir, pdf);
+      } else {
+        pdf = phase_hg(dot(-raydir, ldir), aniso);
+        f = f3(pdf);
+      }
+      float w = 0.0f;
+      bool add = false;
+      if (pdf > 0.0f) {
+        w = power_heuristic(light_pdf, pdf);
+        add = w > 0.0f;
+      }
+      pend |= PEND_ENV;
+      P.sh_d0[p] = make_float4(ldir.x, ldir.y, ldir.z, w);
+      P.sh_c0[p] = make_float4(em.x, em.y, em.z, light_pdf);
+      P.sh_f0[p] = make_float4(f.x, f.y, f.z, add ? 1.0f : 0.0f);
+    }
+  }
+  uint32_t nl = S.num_lights;
+  if (nl > 0) {
+    int li = (int)(rand1(rng) * (float)nl);
+    DevLight L = {};
+    if (li >= 0 && li < (int)nl) L = S.lights[li];
+    LightSample ls = sample_light(rng, fhp, L, nl);
+    float light_pdf = ls.pdf;
+    if (light_pdf > 0.0f && dot(ls.direction, ls.normal) < 0.0f) {
+      float pdf = 0.0f;
+      float3 f = f3(0.0f);
+      if (is_surface) {
+        f = bsdf_eval<MAT, false>(st.fr, mat, ans, -raydir, st.ffnormal, ls.direction, pdf);
+      } else {
+        pdf = phase_hg(dot(-raydir, ls.direction), aniso);
+        f = f3(pdf);
+      }
+      float w = 1.0f;
+      bool add = false;
+      if (pdf > 0.0f) {
+        if (L.area > 0.0f) w = power_heuristic(light_pdf, pdf);
+        add = w > 0.0f;
+      }
+      pend |= PEND_LIGHT;
+      P.sh_d1[p] = make_float4(ls.direction.x, ls.direction.y, ls.direction.z, w);
+      P.sh_c1[p] = make_float4(ls.emission.x, ls.emission.y, ls.emission.z, light_pdf);
+      P.sh_f1[p] = make_float4(f.x, f.y, f.z, add ? 1.0f : 0.0f);
+    }
+  }
+  if (pend) {
+    P.sh_o[p] = make_float4(scatter_pos.x, scatter_pos.y, scatter_pos.z, 0.0f);
+    P.sh_T[p] = make_float4(T.x, T.y, T.z, 0.0f);
+  }
+  return pend;
+}
 
 // Closest hit of path p's ray and the class of what it hit: 0 for a miss,
 // an emitter or an invalid material (surface logic), else MAT_CLASS_*
@@ -475,6 +561,51 @@ __device__ __forceinline__ uint32_t shadow_path(const DevScene& S0, const PathSt
   float3 rad = f3(r4) + f3(P.sh_T[p]) * Ld;
   P.rad[p] = make_float4(rad.x, rad.y, rad.z, __uint_as_float(hash));
   return nrays;
+}
+
+// The deferred next-event rays of a vertex with media (prepare_volmis):
+// transmittance of each pending ray, its visibility event, and the light it
+// adds, in the order and arithmetic of direct_lighting_volmis; then the
+// hash events that wait for them. Returns the closest-hit rays traced.
+template <bool MULTI>
+__device__ __forceinline__ uint32_t transmit_path(const DevScene& S0, const PathState& P, uint32_t p) {
+  const DevScene& S = MULTI ? P.jobs[P.job[p]] : S0;
+  float4 so = P.sh_o[p];
+  uint32_t pend = __float_as_uint(so.w);
+  float3 o = f3(so);
+  float4 r4 = P.rad[p];
+  uint32_t hash = __float_as_uint(r4.w);
+  float3 Ld = f3(0.0f);
+  unsigned long long nrays = 0;
+  uint4 no_rng = make_uint4(0u, 0u, 0u, 0u);  // not drawn from without transparent materials
+  if (pend & PEND_ENV) {
+    const float4 d0 = P.sh_d0[p], c0 = P.sh_c0[p], f0 = P.sh_f0[p];
+    const float3 T = transmittance<false>(S, no_rng, o, f3(d0), nrays);
+    const bool vis = luminance(T) > 0.0f;
+    hmix(hash, 0x40000000u | (vis ? 1u : 0u));
+    if (vis && f0.w != 0.0f) {
+      float3 Li = f3(c0);
+      Li *= T;
+      Ld += d0.w * Li * f3(f0) / c0.w;
+    }
+  }
+  if (pend & PEND_LIGHT) {
+    const float4 d1 = P.sh_d1[p], c1 = P.sh_c1[p], f1 = P.sh_f1[p];
+    const float3 T = transmittance<false>(S, no_rng, o, f3(d1), nrays);
+    const bool vis = luminance(T) > 0.0f;
+    hmix(hash, 0x50000000u | (vis ? 1u : 0u));
+    if (vis && f1.w != 0.0f) {
+      float3 Li = f3(c1);
+      Li *= T;
+      Ld += d1.w * Li * f3(f1) / c1.w;
+    }
+  }
+  if (pend & PEND_BSDF) hmix(hash, 0x60000000u | ((pend >> 8) & 0xFFFu));
+  if (pend & PEND_STOP) hmix(hash, 0x61000000u);
+  if (pend & PEND_RR) hmix(hash, 0x72000000u);
+  float3 rad = f3(r4) + f3(P.sh_T[p]) * Ld;
+  P.rad[p] = make_float4(rad.x, rad.y, rad.z, __uint_as_float(hash));
+  return (uint32_t)nrays;
 }
 
 // Warp-aggregated append that returns the slot index (or ~0u when !pred).
@@ -620,7 +751,12 @@ __device__ __forceinline__ ShadeResult shade_path(const DevScene& S0, const Path
           T *= mcol;
           o = o + d * sd;
           fhp = o;
-          rad += sh.template direct_lighting_volmis<TRANSPARENT>(mat, false, ans, st, fhp, d, m1.x) * T;
+          if (TRANSPARENT) {
+            rad += sh.template direct_lighting_volmis<TRANSPARENT>(mat, false, ans, st, fhp, d, m1.x) * T;
+          } else {
+            pend |= sh.prepare_volmis(P, p, mat, false, ans, st, fhp, d, m1.x, T);
+            if (!pend) rad += f3(0.0f) * T;  // no ray pending: Ld = 0 (NaN for a non-finite T)
+          }
           float q1 = rand1(sh.rng);
           float q2 = rand1(sh.rng);
           float3 sdir = sample_hg(-d, m1.x, q1, q2);
@@ -639,8 +775,11 @@ __device__ __forceinline__ ShadeResult shade_path(const DevScene& S0, const Path
         }
       }
       if (!skip) {
-        if (MEDIUM) {
+        if (MEDIUM && TRANSPARENT) {
           rad += T * sh.template direct_lighting_volmis<TRANSPARENT>(mat, true, ans, st, fhp, d, m1.x);
+        } else if (MEDIUM) {
+          pend |= sh.prepare_volmis(P, p, mat, true, ans, st, fhp, d, m1.x, T);
+          if (!pend) rad += T * f3(0.0f);
         } else {
           // Next-event estimation with deferred visibility (inc/lighting.glsl:69-244).
           float3 scatter_pos = fhp + st.ffnormal * EPS;
@@ -748,7 +887,7 @@ __device__ __forceinline__ ShadeResult shade_path(const DevScene& S0, const Path
     }
     // hash events of the BSDF sample / termination, unless the shadow kernel
     // has to put the visibility events first
-    bool deferred = !MEDIUM && (pend & (PEND_ENV | PEND_LIGHT));
+    bool deferred = !(MEDIUM && TRANSPARENT) && (pend & (PEND_ENV | PEND_LIGHT));
     if (!deferred) {
       if (pend & PEND_BSDF) hmix(sh.hash, 0x60000000u | ((pend >> 8) & 0xFFFu));
       if (pend & PEND_STOP) hmix(sh.hash, 0x61000000u);
@@ -844,7 +983,7 @@ __global__ void __launch_bounds__(TAIL_BLOCK) k_tail(const __grid_constant__ Dev
           r = tail_shade<PT_MATERIAL_DISNEY, MEDIUM, TRANSPARENT, MULTI, TEXTURED, CACHE>(S0, P, p, nshadow);
         else
           r = tail_shade<SHADE_DISNEY_GLASS, MEDIUM, TRANSPARENT, MULTI, TEXTURED, CACHE>(S0, P, p, nshadow);
-        if (r.deferred) nshadow += shadow_path<false, MULTI>(S0, P, p);
+        if (r.deferred) nshadow += MEDIUM ? transmit_path<MULTI>(S0, P, p) : shadow_path<false, MULTI>(S0, P, p);
         live = !r.stop;
       }
     }

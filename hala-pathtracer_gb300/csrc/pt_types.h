@@ -138,13 +138,20 @@ struct PathState {
   float4* normal;    // first-hit normal
   float4* med0;      // medium color.xyz, density
   float2* med1;      // medium anisotropy, type bits
-  // pending next-event estimation (non-VOL_MIS): shadow rays + contributions
-  float4* sh_o;      // scatter position, mask bits (1 env, 2 light), events
+  // pending next-event estimation: shadow rays + contributions. Surfaces
+  // without media (k_shadow):
+  float4* sh_o;      // scatter position, pending bits (1 env, 2 light) and events
   float4* sh_d0;     // env ray dir, tmax
   float4* sh_d1;     // light ray dir, tmax
   float4* sh_c0;     // env contribution, (unused)
-  float4* sh_c1;     // light contribution, pending hash events
+  float4* sh_c1;     // light contribution, (unused)
   float4* sh_T;      // throughput at the NEE vertex
+  // With media and no transparent material (k_transmit): sh_d0/sh_d1 hold
+  // the ray direction and MIS weight, sh_c0/sh_c1 the light's radiance and
+  // pdf, sh_f0/sh_f1 the BSDF or phase value and whether the sample adds
+  // light when visible (media waves only).
+  float4* sh_f0;
+  float4* sh_f1;
   // shared wavefronts of several jobs (serving): per-path job slot and the
   // device table of the jobs' scene records; null for a single-scene render
   uint32_t* job;
