@@ -195,7 +195,8 @@ class Renderer:
 
     def set_tail_paths(self, paths):
         """Live paths at or below which a wave's remaining bounces run as one
-        kernel (0: never); the images do not depend on it."""
+        kernel (0: never; abi.TAIL_PATHS_AUTO: chosen from the scene, the
+        default); the images do not depend on it."""
         self._check(self._lib.pt_renderer_set_tail_paths(self._h, int(paths)))
 
     def set_traversal_limits(self, stack_entries=0, max_visits=0):

@@ -162,6 +162,7 @@ PROFILE_COUNT = 2
 PROFILE_HOST_LOOP = 4
 NOALLOC_MAX_TRIANGLES = 65536
 BVH_BUILD_SAH, BVH_BUILD_FAST = 0, 1
+TAIL_PATHS_AUTO = 0xFFFFFFFF
 
 
 def make_config(width, height, max_depth=8, rr_depth=0, enable_tonemap=True, enable_aces=True,

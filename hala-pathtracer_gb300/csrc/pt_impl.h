@@ -200,7 +200,8 @@ struct pt_renderer {
   uint32_t profiling = 0;
   std::vector<cudaEvent_t> tev;  // start/stop pairs around closest-hit launches
   uint32_t bvh_build = PT_BVH_BUILD_SAH;  // pt_renderer_set_bvh_build
-  uint32_t tail_paths = 16384;             // pt_renderer_set_tail_paths
+  uint32_t tail_paths = PT_TAIL_PATHS_AUTO; // pt_renderer_set_tail_paths
+  bool has_glass = false;                  // some material can sample the glass lobe
   // traversal limits and the device word their violations set (TRAV_ERR_*)
   uint32_t trav_stack = 96, trav_visits = 1u << 22;
   hpt::Buf<uint32_t> errw;

@@ -336,14 +336,18 @@ pt_status pt_renderer_set_bvh_build(pt_renderer* r, uint32_t mode);
 /* Wave tail (no counterpart in the reference): once at most `paths` paths
  * of a wavefront are still alive, their remaining bounces run as one kernel
  * launch, one thread carrying each path to its end, instead of one launch
- * chain per bounce whose time the slowest ray sets. 0 turns it off; the
- * default is 16384. The bounce graph switches at its grid sizes (4096 x 4^k
+ * chain per bounce whose time the slowest ray sets. 0 turns it off;
+ * PT_TAIL_PATHS_AUTO (the default) picks 16384 when some material can
+ * refract (a glass lobe) or the scene has media, whose long chains of
+ * bounces keep one tail thread busy longest, else 65536. The bounce graph
+ * switches at its grid sizes (4096 x 4^k
  * paths), so the threshold in effect there is the largest such size not
  * above `paths`. Images, ray counts and bounce counts are the same either
  * way (with a radiance cache attached, the cache's training samples are
  * gathered in another order, so its images agree to within its training
  * noise). The PT_PROFILE_TRACE_TIMING / PT_PROFILE_COUNT instrumentation
  * always uses the per-bounce launches. */
+#define PT_TAIL_PATHS_AUTO 0xFFFFFFFFu
 pt_status pt_renderer_set_tail_paths(pt_renderer* r, uint32_t paths);
 
 /* Traversal limits of this renderer: stack entries per ray (1..96; 0 = 96)
