@@ -64,7 +64,6 @@ cudaError_t WaveBuffers::ensure(uint32_t want, bool want_med, bool want_multi) {
   chk(sh_T.ensure(want));
   chk(q_a.ensure(want));
   chk(q_b.ensure(want));
-  chk(q_logic.ensure(want));
   chk(q_diff.ensure(want));
   chk(q_dis.ensure(want));
   chk(q_glass.ensure(want));
@@ -107,7 +106,7 @@ void WaveBuffers::release() {
                        &sh_o, &sh_d0, &sh_d1, &sh_c0, &sh_c1, &sh_T, &sh_f0, &sh_f1};
   for (auto* b : f4) b->release();
   med1.release();
-  Buf<uint32_t>* u[] = {&depth, &flags, &job, &q_a, &q_b, &q_logic, &q_diff, &q_dis, &q_glass, &q_shadow, &counters};
+  Buf<uint32_t>* u[] = {&depth, &flags, &job, &q_a, &q_b, &q_diff, &q_dis, &q_glass, &q_shadow, &counters};
   for (auto* b : u) b->release();
   rays.release();
   cap = 0;
@@ -117,9 +116,9 @@ void WaveBuffers::release() {
 
 uint64_t WaveBuffers::bytes_per_path(bool med, bool multi) {
   // rng 16, ray_o/ray_d/hit/thr/rad/albedo/normal 7x16, depth+flags 8,
-  // six NEE float4 96, seven queues 28 (+ medium 24 and two NEE float4 32,
+  // six NEE float4 96, six queues 24 (+ medium 24 and two NEE float4 32,
   // + job slot 4)
-  return 16 + 7 * 16 + 8 + 96 + 28 + (med ? 56 : 0) + (multi ? 4 : 0);
+  return 16 + 7 * 16 + 8 + 96 + 24 + (med ? 56 : 0) + (multi ? 4 : 0);
 }
 
 cudaError_t run_bounces(const DevScene& S, WaveBuffers& W, uint32_t live, uint32_t max_depth, BounceLoop& L,
@@ -127,10 +126,10 @@ cudaError_t run_bounces(const DevScene& S, WaveBuffers& W, uint32_t live, uint32
   uint32_t* cnt0 = W.counters.p;
   uint32_t* cnt1 = W.counters.p + Q_COUNT;
   const uint32_t bounce_cap = 4u * max_depth + 4096u;
-  // trace, logic, 3 shades, and shadow rays (k_shadow, or k_transmit with
-  // media unless a material is transparent)
+  // trace, 3 shades, and shadow rays (k_shadow, or k_transmit with media
+  // unless a material is transparent)
   const bool med_tr = (S.features & PT_FEATURE_MEDIUM) && (S.features & PT_FEATURE_TRANSPARENT);
-  const uint64_t per_bounce = med_tr ? 5 : 6;
+  const uint64_t per_bounce = med_tr ? 4 : 5;
   if (live == 0) {
     L.bounces = 0;
     L.timed_out = false;
@@ -149,7 +148,7 @@ cudaError_t run_bounces(const DevScene& S, WaveBuffers& W, uint32_t live, uint32
     uint32_t* qnext = (b & 1) ? W.q_a.p : W.q_b.p;
     cudaError_t e = cudaMemsetAsync(out, 0, Q_COUNT * sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
-    QueueSet Q{qin, in_cnt, qnext, W.q_logic.p, W.q_diff.p, W.q_dis.p, W.q_glass.p, W.q_shadow.p, out,
+    QueueSet Q{qin, in_cnt, qnext, W.q_diff.p, W.q_dis.p, W.q_glass.p, W.q_shadow.p, out,
                  W.rays.p};
     if (live <= tail) {
       // the rest of the wave in one kernel: the loop ends here

@@ -93,7 +93,7 @@ QueueSet queues_for(WaveBuffers& W, uint32_t parity) {
   uint32_t* in_cnt = (parity ? cnt0 : cnt1) + Q_NEXT;
   uint32_t* qin = parity ? W.q_b.p : W.q_a.p;
   uint32_t* qnext = parity ? W.q_a.p : W.q_b.p;
-  return QueueSet{qin, in_cnt, qnext, W.q_logic.p, W.q_diff.p, W.q_dis.p, W.q_glass.p, W.q_shadow.p, out,
+  return QueueSet{qin, in_cnt, qnext, W.q_diff.p, W.q_dis.p, W.q_glass.p, W.q_shadow.p, out,
                   W.rays.p};
 }
 
@@ -253,7 +253,7 @@ cudaError_t run_bounces_graph(const DevScene& S, WaveBuffers& W, uint32_t bounce
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
   const uint32_t done = pinned[G_DONE], live = pinned[G_LIVE], tail_bounces = pinned[G_TAIL];
   const bool med_tr = (S.features & PT_FEATURE_MEDIUM) && (S.features & PT_FEATURE_TRANSPARENT);
-  const uint64_t per_bounce = med_tr ? 5 : 6;
+  const uint64_t per_bounce = med_tr ? 4 : 5;
   const uint64_t cases = done - tail_bounces + (tail_bounces ? 1 : 0);  // switch cases that ran
   L.bounces = done;
   L.timed_out = live > 0;

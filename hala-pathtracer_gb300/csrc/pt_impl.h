@@ -92,7 +92,7 @@ struct WaveBuffers {
   Buf<float2> med1;
   Buf<float4> sh_o, sh_d0, sh_d1, sh_c0, sh_c1, sh_T, sh_f0, sh_f1;
   Buf<uint32_t> depth, flags, job;
-  Buf<uint32_t> q_a, q_b, q_logic, q_diff, q_dis, q_glass, q_shadow, counters;
+  Buf<uint32_t> q_a, q_b, q_diff, q_dis, q_glass, q_shadow, counters;
   Buf<unsigned long long> rays;
   PathState P{};
   BounceGraph graph;

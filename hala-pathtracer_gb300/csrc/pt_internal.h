@@ -13,7 +13,6 @@ struct QueueSet {
   const uint32_t* in;        // active paths of this bounce
   const uint32_t* in_count;  // their number
   uint32_t* next;            // paths continuing to the next bounce
-  uint32_t* logic;
   uint32_t* diffuse;
   uint32_t* disney;
   uint32_t* glass;

@@ -3,10 +3,11 @@
 // One wavefront = a contiguous range of global path indices
 // g = frame_local * (W*H) + pixel. Per bounce the kernels run in this order:
 //
-//   k_trace        closest hit for every active path (pathtracer.rgen.glsl:56-68)
-//                  and sorts the path into a queue by what it hit
-//   k_shade_logic  miss -> environment, emitter hit -> MIS, invalid material
-//                  (pathtracer.rgen.glsl:70-115)
+//   k_trace        closest hit for every active path (pathtracer.rgen.glsl:56-68);
+//                  a miss (environment), an emitter hit (MIS) or an invalid
+//                  material (pathtracer.rgen.glsl:70-115) ends the path right
+//                  there, any other hit sorts the path into the queue of its
+//                  material class
 //   k_shade<MAT>   one kernel per material type (diffuse / Disney): emission,
 //                  media, transparency, next-event estimation, BSDF sampling,
 //                  Russian roulette (pathtracer.rgen.glsl:117-256)
@@ -130,6 +131,14 @@ __global__ void k_camera_multi(PathState P, const WaveSegment* segs, uint32_t ns
 // ------------------------------------------------------------------ trace
 constexpr uint32_t TRACE_BLOCK = 256;
 
+// The surface logic of a path whose ray missed, hit an emitter or an invalid
+// material, called from k_trace after its traversal (out of line, so that
+// the traversal loop keeps its registers).
+template <bool MULTI>
+__device__ __noinline__ void logic_call(const DevScene& S0, const PathState& P, uint32_t p) {
+  logic_path<MULTI>(S0, P, p);
+}
+
 template <bool BRUTE, bool COUNT, bool MULTI>
 __global__ void __launch_bounds__(TRACE_BLOCK, 5) k_trace(const __grid_constant__ DevScene S0, PathState P,
                                                           QueueSet Q) {
@@ -138,7 +147,7 @@ __global__ void __launch_bounds__(TRACE_BLOCK, 5) k_trace(const __grid_constant_
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const uint32_t p = Q.in[i];
     const uint32_t cls = trace_path<BRUTE, COUNT, MULTI>(S0, P, p, tc);
-    queue_push(Q.logic, &Q.counts[Q_LOGIC], p, cls == 0);
+    if (cls == 0) logic_call<MULTI>(S0, P, p);  // miss / emitter / invalid material: the path ends here
     queue_push(Q.diffuse, &Q.counts[Q_DIFFUSE], p, cls == MAT_CLASS_DIFFUSE);
     queue_push(Q.disney, &Q.counts[Q_DISNEY], p, cls == MAT_CLASS_DISNEY);
     queue_push(Q.glass, &Q.counts[Q_GLASS], p, cls == MAT_CLASS_GLASS);
@@ -292,13 +301,11 @@ void launch_shade(const DevScene& S, const PathState& P, const QueueSet& Q, uint
   const bool tr = (S.features & PT_FEATURE_TRANSPARENT) != 0;
   const bool tex = (S.features & PT_FEATURE_TEXTURED) != 0;
   if (P.job) {
-    k_shade_logic<true><<<g, 256, 0, st>>>(S, P, Q);
     if (med) launch_materials_multi_medium(S, P, Q, g, tr, tex, st);
     else launch_materials_multi(S, P, Q, g, tr, tex, st);
     if (!med) k_shadow<false, true><<<g, 256, 0, st>>>(S, P, Q);
     else if (!tr) k_transmit<true><<<g, 256, 0, st>>>(S, P, Q);
   } else {
-    k_shade_logic<false><<<g, 256, 0, st>>>(S, P, Q);
     if (med) launch_materials_medium(S, P, Q, g, tr, tex, st);  // the cache is refused for scenes with media
     else if (P.c_rec != nullptr) launch_materials_cache(S, P, Q, g, tr, tex, st);
     else launch_materials_plain(S, P, Q, g, tr, tex, st);

@@ -308,13 +308,6 @@ __device__ __forceinline__ void logic_path(const DevScene& S0, const PathState& 
   }
 }
 
-template <bool MULTI>
-__global__ void __launch_bounds__(256) k_shade_logic(const __grid_constant__ DevScene S0, PathState P, QueueSet Q) {
-  const uint32_t n = Q.counts[Q_LOGIC];
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    logic_path<MULTI>(S0, P, Q.logic[i]);
-}
-
 // inc/lighting.glsl:7-61 (MEDIUM && VOL_MIS): transmittance along a shadow
 // ray through refractive (and, with TRANSPARENT, transparent) surfaces and
 // the media behind them. Draws random numbers only with TRANSPARENT; counts

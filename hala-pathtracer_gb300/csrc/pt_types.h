@@ -196,7 +196,7 @@ constexpr int SHADE_DISNEY_GLASS = 2;
 // Queue counters (device memory)
 enum QueueSlot : int {
   Q_NEXT = 0,     // paths continuing to the next bounce
-  Q_LOGIC = 1,    // miss / emitter / invalid-material hits
+  // slot 1 unused (misses and emitter hits end in the closest-hit kernel)
   Q_DIFFUSE = 2,  // surface hits on diffuse materials
   Q_DISNEY = 3,   // surface hits on Disney materials without a glass lobe
   Q_SHADOW = 4,   // paths with pending shadow rays
