@@ -643,8 +643,9 @@ static __device__ __forceinline__ float3 disney_eval_body(bool ans, const ShadeF
 }
 
 // One out-of-line copy per kernel instead of one per call site. The kernels of
-// scenes with media (which also hold the in-thread transmittance traversal)
-// run faster with it (media box +4%), the others with the body inlined (Disney
+// scenes with media ran faster with it (media box +4%, measured while they
+// also held the transmittance traversal that k_transmit now runs for scenes
+// without transparent materials), the others with the body inlined (Disney
 // grid +2%).
 template <bool GLASS>
 static __device__ __noinline__ float3 disney_eval_call(bool ans, const ShadeFrame& s, const pt_material& m, float3 V,

@@ -13,10 +13,15 @@
 //                  Russian roulette (pathtracer.rgen.glsl:117-256)
 //   k_shadow       shadow rays of the pending next-event estimation and the
 //                  radiance update it implies (inc/lighting.glsl:116-149, 203-238)
+//   k_transmit     instead of k_shadow in scenes with media: the transmittance
+//                  rays of next-event estimation (inc/lighting.glsl:7-61)
 //
-// Scenes with media use VOL_MIS like the reference host (src/bin/hala-pathtracer.rs:102-103):
-// their transmittance loop (inc/lighting.glsl:7-61) draws from the path RNG
-// between light samples, so the shade kernel evaluates it in-thread.
+// Scenes with media use VOL_MIS like the reference host (src/bin/hala-pathtracer.rs:102-103).
+// With a transparent material their transmittance loop draws from the path
+// RNG between the light samples, so the shade kernel evaluates it in-thread;
+// without one it draws nothing and is deferred to k_transmit.
+// Once few paths of a wave are left, k_tail (pt_shade.cuh) runs their
+// remaining bounces in one launch.
 //
 // Every kernel is a grid-stride loop over a queue whose length lives in
 // device memory, so a bounce needs no host round trip.
