@@ -684,14 +684,21 @@ pt_status pt_renderer_set_scene(pt_renderer* r, const pt_scene_desc* s) {
   CK(r, r->raw_verts.ensure(11 * (size_t)std::max<uint64_t>(nv, 1)));
   CK(r, r->raw_idx.ensure(3 * (size_t)std::max<uint64_t>(nt, 1)));
   CK(r, r->dprims.ensure(std::max<size_t>(prims.size(), 1)));
-  for (uint32_t i = 0; i < s->num_primitives; ++i) {
-    const pt_primitive& p = s->primitives[i];
-    if (p.num_vertices)
-      CK(r, cudaMemcpyAsync(r->raw_verts.p + 11 * (size_t)prims[i].vbase, p.vertices,
-                            11 * sizeof(float) * (size_t)p.num_vertices, cudaMemcpyHostToDevice, st));
-    if (p.num_indices)
-      CK(r, cudaMemcpyAsync(r->raw_idx.p + 3 * (size_t)prims[i].tbase, p.indices, sizeof(uint32_t) * p.num_indices,
-                            cudaMemcpyHostToDevice, st));
+  {
+    // every primitive's vertices and indices packed back to back on the host,
+    // then one copy each: one call per primitive costs more than the bytes
+    // (a copy from pageable memory has taken its source when it returns)
+    std::vector<float> hv(11 * (size_t)nv);
+    std::vector<uint32_t> hi(3 * (size_t)nt);
+    for (uint32_t i = 0; i < s->num_primitives; ++i) {
+      const pt_primitive& p = s->primitives[i];
+      if (p.num_vertices)
+        std::memcpy(hv.data() + 11 * (size_t)prims[i].vbase, p.vertices, 11 * sizeof(float) * (size_t)p.num_vertices);
+      if (p.num_indices)
+        std::memcpy(hi.data() + 3 * (size_t)prims[i].tbase, p.indices, sizeof(uint32_t) * p.num_indices);
+    }
+    if (nv) CK(r, cudaMemcpyAsync(r->raw_verts.p, hv.data(), hv.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+    if (nt) CK(r, cudaMemcpyAsync(r->raw_idx.p, hi.data(), hi.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
   }
   if (!prims.empty())
     CK(r, cudaMemcpyAsync(r->dprims.p, prims.data(), prims.size() * sizeof(PrimUpload), cudaMemcpyHostToDevice, st));
