@@ -116,7 +116,7 @@ class CacheConfig(C.Structure):
                 ("log2_table_size", C.c_uint32), ("learning_rate", C.c_float),
                 ("min_resolution", C.c_uint32), ("max_resolution", C.c_uint32), ("seed", C.c_uint32),
                 ("warmup_frames", C.c_uint32), ("paths_per_pass", C.c_uint32), ("steps_per_pass", C.c_uint32),
-                ("weight_grad_kernel", C.c_uint32)]
+                ("weight_grad_kernel", C.c_uint32), ("min_roughness", C.c_float)]
 
 
 class ServerConfig(C.Structure):

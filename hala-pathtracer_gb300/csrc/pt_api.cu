@@ -517,6 +517,7 @@ pt_status cache_prepare(pt_renderer* r, uint32_t cap) {
   P.t_R = r->t_R.p;
   P.c_depth = r->cache_cfg.query_depth;
   P.c_shift = r->cache_cfg.train_shift;
+  P.c_min_rough = r->cache_cfg.min_roughness;
   P.c_mode = 2;
   return PT_OK;
 }
@@ -1087,6 +1088,7 @@ pt_status pt_renderer_set_radiance_cache(pt_renderer* r, const pt_cache_config* 
   if (cfg->paths_per_pass) c.paths_per_pass = cfg->paths_per_pass;
   c.steps_per_pass = cfg->steps_per_pass;
   c.weight_grad_kernel = cfg->weight_grad_kernel;
+  c.min_roughness = cfg->min_roughness;
   c.seed = cfg->seed;
   if (c.query_depth == 0) return fail(r, PT_ERR_INVALID_ARG, "query_depth must be at least 1");
   if (c.train_shift > 16) return fail(r, PT_ERR_INVALID_ARG, "train_shift must be at most 16");

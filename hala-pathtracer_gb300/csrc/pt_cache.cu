@@ -811,6 +811,7 @@ void pt_cache_config_default(pt_cache_config* c) {
   c->warmup_frames = 1;
   c->paths_per_pass = 1u << 21;
   c->steps_per_pass = 1;
+  c->min_roughness = 0.3f;
 }
 
 pt_status pt_cache_create(const pt_cache_config* cfg, pt_cache** out) {

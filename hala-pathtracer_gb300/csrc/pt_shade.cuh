@@ -691,7 +691,13 @@ __device__ __forceinline__ ShadeResult shade_path(const DevScene& S0, const Path
     // either the cache's estimate -- the path ends here and the estimate is
     // added after the bounce loop -- or, for a training path, traced on.
     bool cache_query = false;
-    if (CACHE && depth == P.c_depth) {
+    // Only diffuse-looking vertices use the cache: at a glossy or refracting
+    // vertex the light through the BSDF is a narrow, view-dependent lobe whose
+    // training targets are heavy-tailed glints, so such a path goes on
+    // unbiased and does not train.
+    const bool cache_vertex = MAT == PT_MATERIAL_DIFFUSE ||
+                              (MAT == PT_MATERIAL_DISNEY && !(mat.roughness < P.c_min_rough));
+    if (CACHE && depth == P.c_depth && cache_vertex) {
       const float4 rec0 = make_float4(st.fhp.x, st.fhp.y, st.fhp.z, -d.x);
       const float4 rec1 = make_float4(-d.y, -d.z, st.ffnormal.x, st.ffnormal.y);
       const float4 rec2 = make_float4(st.ffnormal.z, mat.base_color[0], mat.base_color[1], mat.base_color[2]);

@@ -169,6 +169,7 @@ struct PathState {
   uint32_t c_depth;    // vertex index of the query
   uint32_t c_mode;     // 1 = every path trains (warm-up), 2 = query, 1 in 2^c_shift trains
   uint32_t c_shift;
+  float c_min_rough;   // cache vertices must be at least this rough (and not glass)
 };
 
 // One contiguous run of a job's paths inside a shared wavefront: wave slots

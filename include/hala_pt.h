@@ -564,11 +564,15 @@ struct pt_cache_config {
   uint32_t weight_grad_kernel; /* weight gradients: 0 = tcgen05 tensor-core kernel with the
                                   accumulator in tensor memory, 1 = the warp-level mma.sync
                                   kernel (kept for comparison) */
+  float min_roughness;      /* the cache vertex queries (or trains) the cache only where the
+                               surface is diffuse, or Disney without a glass lobe and at least
+                               this rough; elsewhere the path goes on unbiased. 0 = every vertex */
 };
 
 /* query_depth 1, 1/32 training paths, batch 65536, 2^19 entries, lr 1e-2,
  * resolutions 16..2048, seed 1, one warm-up frame, passes of 2^21 paths,
- * at least one optimiser step per pass, tcgen05 weight gradients. */
+ * at least one optimiser step per pass, tcgen05 weight gradients, cache
+ * vertices at least 0.3 rough. */
 void pt_cache_config_default(pt_cache_config* config);
 pt_status pt_cache_create(const pt_cache_config* config, pt_cache** out);
 void pt_cache_destroy(pt_cache* cache);
