@@ -191,6 +191,29 @@ def test_renderer_with_cache(pt, scenes):
 
 
 @pytest.mark.gpu
+def test_cache_skips_glossy_and_glass_vertices(pt, scenes):
+    """The cache vertex is used only where the surface is diffuse, or Disney
+    without a glass lobe and at least min_roughness rough. On the Disney grid
+    with min_roughness above every material's roughness no vertex qualifies:
+    nothing is queried or trained, and the image is the plain tracer's bit
+    for bit; with the default some vertices qualify."""
+    sc = scenes.tiny_variants()["disney"]
+    plain = pt.renderer_for(sc)
+    plain.render(sc.spp)
+    r = pt.renderer_for(sc)
+    r.set_radiance_cache(min_roughness=2.0, warmup_frames=1)
+    r.render(sc.spp)
+    st = r.stats()
+    assert st.cache_queries == 0 and st.cache_train_samples == 0
+    for k in range(4):
+        assert np.array_equal(r.image(k).view(np.uint8), plain.image(k).view(np.uint8)), f"image {k} differs"
+    r2 = pt.renderer_for(sc)
+    r2.set_radiance_cache(warmup_frames=0)
+    r2.render(sc.spp)
+    assert r2.stats().cache_queries > 0
+
+
+@pytest.mark.gpu
 def test_cache_rmse_against_the_fp64_oracle(pt, scenes):
     """What the trained cache changes against the plain tracer on the
     Cornell box, judged against the 4096-spp FP64 oracle image: paths end
