@@ -45,14 +45,14 @@ def _pin_scene(name):
                                   "pin:media_transparent"])
 def test_wave_tail_matches_wavefront(pt, abi, scenes, name):
     """The wave tail (one kernel carrying each remaining path to its end)
-    against the per-bounce wavefront: off, the default threshold, and every
-    bounce of every wave in the tail, with the bounce graph and the host
+    against the per-bounce wavefront: off, the automatic threshold, 4096,
+    and every bounce of every wave in the tail, with the bounce graph and the host
     loop, over small and large wavefronts. Images, ray counts and bounce
     counts must be identical."""
     sc = _pin_scene(name[4:]) if name.startswith("pin:") else scenes.tiny_variants()[name]
     ref, sref = _render(pt, abi, sc, abi.PROFILE_HOST_LOOP, sc.spp, tail=0, wave_paths=70000)
     for flags in (0, abi.PROFILE_HOST_LOOP):
-        for tail in (4096, 1 << 31):
+        for tail in (abi.TAIL_PATHS_AUTO, 4096, 1 << 31):
             for wave in (0, 5000):
                 b, sb = _render(pt, abi, sc, flags, sc.spp, tail=tail, wave_paths=wave)
                 where = f"flags {flags} tail {tail} wave {wave}"
