@@ -244,8 +244,8 @@ __device__ __forceinline__ HitRec trace_tris_closest(const DevScene& S, float3 o
   }
   if (S.num_tris == 0) return h;
   const SlabRay sr = slab_ray(o, d);
-  int32_t st_link[TRAV4_STACK];
-  float st_t[TRAV4_STACK];
+  // (entry distance, link) pairs: one 8-byte local access per push or pop
+  float2 st[TRAV4_STACK];
   int sp = 0;
   const int lim = (int)min(S.trav_stack, (uint32_t)TRAV4_STACK);
   int32_t cur = 0;  // root is always internal
@@ -283,8 +283,9 @@ __device__ __forceinline__ HitRec trace_tris_closest(const DevScene& S, float3 o
         cur = 0x7FFFFFFF;
         while (sp > 0) {
           --sp;
-          if (st_t[sp] <= h.t * TRAV_T_SLACK) {
-            cur = st_link[sp];
+          const float2 e = st[sp];
+          if (e.x <= h.t * TRAV_T_SLACK) {
+            cur = __float_as_int(e.y);
             break;
           }
         }
@@ -295,8 +296,7 @@ __device__ __forceinline__ HitRec trace_tris_closest(const DevScene& S, float3 o
 #pragma unroll
       for (int j = BVH_WIDTH - 1; j >= 1; --j)
         if (nh > j && sp < lim) {
-          st_link[sp] = v[j];
-          st_t[sp] = k[j];
+          st[sp] = make_float2(k[j], __int_as_float(v[j]));
           ++sp;
         }
       cur = v0;
@@ -315,8 +315,9 @@ __device__ __forceinline__ HitRec trace_tris_closest(const DevScene& S, float3 o
     cur = 0x7FFFFFFF;
     while (sp > 0) {
       --sp;
-      if (st_t[sp] <= h.t * TRAV_T_SLACK) {
-        cur = st_link[sp];
+      const float2 e = st[sp];
+      if (e.x <= h.t * TRAV_T_SLACK) {
+        cur = __float_as_int(e.y);
         break;
       }
     }
