@@ -48,9 +48,12 @@ WORKLOADS = {
 }
 DEFAULT_WORKLOAD = "disney_grid_1080p_64spp"
 L2_FLUSH_BYTES = 256 << 20  # > 129 MB L2
-# DRAM bytes (read + write) per closest-hit ray of k_trace, from the ncu
-# capture in profiles/k_trace_disney_grid_480x270_bvh4.md (bounces 0 and 1).
-TRACE_DRAM_BYTES_PER_RAY = (347.765504e6 + 167.930624e6 + 304.260864e6 + 111.250176e6) / (8294400 + 5583360)
+# DRAM bytes (read + write) per closest-hit ray of k_trace: ncu's DRAM bytes
+# of every k_trace launch of one 480x270x64 render of the Disney grid (its
+# bounces 0-10, MB each, from profiles/k_trace_disney_grid_480x270_bvh4.md)
+# over that render's 19,520,376 closest-hit rays.
+TRACE_DRAM_MB_PER_BOUNCE = (744.49, 851.96, 559.77, 616.26, 419.36, 123.11, 61.27, 42.23, 29.07, 21.45, 15.81)
+TRACE_DRAM_BYTES_PER_RAY = sum(TRACE_DRAM_MB_PER_BOUNCE) * 1e6 / 19520376
 
 
 def _dist():
@@ -642,14 +645,16 @@ def main():
         "roofline": {"kernel": "k_trace (closest hit)", "bound": "hbm", "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic,
-                     "traffic_note": "ncu DRAM bytes per ray (480x270 capture, bounces 0-1) x rays per launch",
+                     "traffic_note": "ncu DRAM bytes per closest-hit ray over every k_trace launch of a 480x270x64 "
+                                     "render x rays per launch",
                      "dram_achieved_gbs": dram_gbs, "dram_frac": dram_gbs / peak,
                      "l2": {"achieved": achieved, "peak": l2_gbs, "frac": achieved / l2_gbs if l2_gbs else None,
                             "peak_kind": "measured here: copies between two 32 MiB buffers resident in L2, replayed "
                                          "from a CUDA graph"},
-                     "limiter": "issue and dependent-load latency: the BVH and triangles stay in L2 (72-81% L2 "
-                                "hit rate), DRAM carries ~67 B per ray; ncu shows 64-66% issue active and 8-11 "
-                                "of 32 lanes active per instruction (divergent traversal lengths)",
+                     "limiter": "issue and dependent-load latency: the BVH and triangles stay in L2 (68-81% L2 "
+                                "hit rate), DRAM carries ~180 B per ray (90 B on bounce 0), mostly path state; ncu "
+                                "shows 62-66% issue active and 8-11 of 32 lanes active per instruction (divergent "
+                                "traversal lengths)",
                      "bytes_per_ray": bytes_per_ray, "nodes_per_ray": nodes_per_ray, "tris_per_ray": tris_per_ray,
                      "avg_launch_ms": avg_launch_ms, "launches": trace_launches,
                      "trace_share_of_step": trace_ms / max(sum(host_ms), 1e-9),
