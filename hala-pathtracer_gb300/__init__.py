@@ -105,6 +105,11 @@ class Renderer:
         self._check(self._lib.pt_renderer_set_envmap_file(self._h, None if path is None else str(path).encode(),
                                                           float(rotation_degrees)))
 
+    def set_scene_file(self, path):
+        """HalaScene::new(scene_file) + set_scene: the glTF 2.0 file read by the
+        library itself (pt_renderer_set_scene_file)."""
+        self._check(self._lib.pt_renderer_set_scene_file(self._h, str(path).encode()))
+
     def set_ground_color(self, rgba):
         self._check(self._lib.pt_renderer_set_ground_color(self._h, _f4(rgba)))
 
@@ -251,6 +256,39 @@ def renderer_for(scene, bvh_build=None, **cfg_over):
     r.set_exposure_value(scene.exposure_value)
     r.commit()
     return r
+
+
+def read_gltf(path):
+    """A glTF 2.0 scene through the library's own reader (pt_gltf_load), copied
+    out as a scenes.Scene: meshes (vertices, indices, column-major transform,
+    material), materials, lights, cameras and textures, plus `skipped_images`
+    (the number of images that were not PNG)."""
+    lib = load_library()
+    h = C.c_void_p()
+    err = C.create_string_buffer(512)
+    st = lib.pt_gltf_load(str(path).encode(), C.byref(h), err, 512)
+    if st != abi.PT_OK:
+        raise PTError(st, err.value.decode())
+    try:
+        d = lib.pt_gltf_scene_desc(h).contents
+        s = scenes.Scene(os.path.splitext(os.path.basename(str(path)))[0])
+        for k in range(d.num_primitives):
+            p = d.primitives[k]
+            v = np.ctypeslib.as_array(p.vertices, (p.num_vertices * 11,)).reshape(-1, 11).copy() \
+                if p.num_vertices else np.zeros((0, 11), np.float32)
+            i = np.ctypeslib.as_array(p.indices, (p.num_indices,)).copy() if p.num_indices else np.zeros(0, np.uint32)
+            s.meshes.append((v, i, np.array(list(p.transform), np.float32), int(p.material_index)))
+        s.materials = [abi.Material.from_buffer_copy(d.materials[k]) for k in range(d.num_materials)]
+        s.lights = [abi.Light.from_buffer_copy(d.lights[k]) for k in range(d.num_lights)]
+        s.cameras = [abi.Camera.from_buffer_copy(d.cameras[k]) for k in range(d.num_cameras)]
+        for k in range(d.num_textures):
+            t = d.textures[k]
+            s.textures.append(np.ctypeslib.as_array(t.rgba, (t.height * t.width * 4,)).reshape(t.height, t.width, 4)
+                              .copy())
+        s.skipped_images = int(lib.pt_gltf_skipped_images(h))
+        return s
+    finally:
+        lib.pt_gltf_free(h)
 
 
 def read_exr(path):

@@ -189,6 +189,11 @@ RENDERER_SIGNATURES = {
     "pt_renderer_set_envmap": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_uint32,
                                          C.c_uint32, C.c_float]),
     "pt_renderer_set_envmap_file": (C.c_int, [C.c_void_p, C.c_char_p, C.c_float]),
+    "pt_renderer_set_scene_file": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "pt_gltf_load": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p), C.c_char_p, C.c_size_t]),
+    "pt_gltf_scene_desc": (C.POINTER(SceneDesc), [C.c_void_p]),
+    "pt_gltf_skipped_images": (C.c_uint32, [C.c_void_p]),
+    "pt_gltf_free": (None, [C.c_void_p]),
     "pt_exr_read_rgb": (C.c_int, [C.c_char_p, C.c_void_p, C.c_size_t, C.POINTER(C.c_uint32),
                                   C.POINTER(C.c_uint32), C.c_char_p, C.c_size_t]),
     "pt_renderer_set_ground_color": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),

@@ -447,6 +447,12 @@ void put_error(char* msg, size_t cap, const std::string& s) {
 
 }  // namespace
 
+namespace hpt {
+bool inflate_zlib(const uint8_t* data, size_t size, std::vector<uint8_t>& out, size_t limit) {
+  return zlib_inflate(data, size, out, limit);
+}
+}  // namespace hpt
+
 extern "C" {
 
 pt_status pt_exr_read_rgb(const char* path, float* rgb, size_t capacity_floats, uint32_t* width, uint32_t* height,

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <vector>
 
 #include "pt_types.h"
 
@@ -22,6 +23,10 @@ struct QueueSet {
 };
 
 int device_sm_count();
+
+// pt_exr.cu: a zlib stream (RFC 1950/1951) into `out`, at most `limit`
+// bytes; false on any format error (also used for PNG image data).
+bool inflate_zlib(const uint8_t* data, size_t size, std::vector<uint8_t>& out, size_t limit);
 
 // pt_render.cu
 void launch_camera(const DevScene& S, const PathState& P, uint64_t g0, uint32_t n, uint32_t* q_active,

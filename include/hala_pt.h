@@ -246,6 +246,11 @@ const char* pt_renderer_last_error(const pt_renderer* r);
 /* HalaRenderer::set_scene (src/bin/hala-pathtracer.rs:198): uploads geometry,
  * materials, lights and cameras. The BVH is built on the device at commit. */
 pt_status pt_renderer_set_scene(pt_renderer* r, const pt_scene_desc* scene);
+/* HalaScene::new(scene_file) + HalaRenderer::set_scene
+ * (src/bin/hala-pathtracer.rs:97-99, :198) with the file itself: reads a
+ * glTF 2.0 scene with pt_gltf_load and calls pt_renderer_set_scene with it.
+ * Unreadable or malformed files return PT_ERR_INVALID_ARG with the reason. */
+pt_status pt_renderer_set_scene_file(pt_renderer* r, const char* path);
 /* HalaRenderer::set_envmap (src/bin/hala-pathtracer.rs:203): equirectangular
  * RGB32F pixels (row 0 = theta 0) and the hdri_rotation in degrees. */
 pt_status pt_renderer_set_envmap(pt_renderer* r, const float* rgb, uint32_t width,
@@ -263,6 +268,26 @@ pt_status pt_renderer_set_envmap_file(pt_renderer* r, const char* path, float ro
  * reference (its exr crate dependency, Cargo.lock:502-504). */
 pt_status pt_exr_read_rgb(const char* path, float* rgb, size_t capacity_floats, uint32_t* width,
                           uint32_t* height, char* error_message, size_t error_capacity);
+/* ---- glTF 2.0 scene files --------------------------------------------------
+ * The reader behind pt_renderer_set_scene_file, for hosts that keep a scene
+ * on the CPU (job server submissions, several renderers): .gltf with external
+ * or data-URI buffers, or .glb. Every TRIANGLES primitive of the default
+ * scene's mesh nodes (world matrix as the primitive transform; smooth normals
+ * and orthogonal tangents where the file has none), pbrMetallicRoughness
+ * materials with the emissive-strength, ior, transmission and clearcoat
+ * extensions and the renderer's material `extras` (any pt_material field by
+ * name, "type", "medium"), PNG textures baked as factor x texel,
+ * KHR_lights_punctual lights with the rectangle / sphere area-light extras
+ * {type, param0, param1}, perspective and orthographic cameras. The
+ * reference's own reader is the `gltf` crate (1.4.1) inside its renderer
+ * crate; this mapping is the library's. */
+typedef struct pt_gltf_scene pt_gltf_scene;
+pt_status pt_gltf_load(const char* path, pt_gltf_scene** out, char* error_message, size_t error_capacity);
+/* The scene in pt_renderer_set_scene's form; its arrays live until pt_gltf_free. */
+const pt_scene_desc* pt_gltf_scene_desc(const pt_gltf_scene* scene);
+/* Images the reader left out (not PNG): the maps that named them stay unset. */
+uint32_t pt_gltf_skipped_images(const pt_gltf_scene* scene);
+void pt_gltf_free(pt_gltf_scene* scene);
 /* HalaRenderer::set_ground_color / set_sky_color (src/bin/hala-pathtracer.rs:205-206). */
 pt_status pt_renderer_set_ground_color(pt_renderer* r, const float rgba[4]);
 pt_status pt_renderer_set_sky_color(pt_renderer* r, const float rgba[4]);

@@ -225,3 +225,47 @@ def test_envmap_file_entry_point(pt, io, tmp_path):
     bad.write_bytes(b"not an exr")
     with pytest.raises(pt.PTError, match="not an OpenEXR"):
         a.set_envmap_file(str(bad), 0.0)
+
+
+@pytest.mark.parametrize("name", ["lights_icosphere", "media", "hand"])
+def test_scene_file_entry_point(pt, io, tmp_path, name):
+    """pt_renderer_set_scene_file (the library's own glTF reader, for hosts
+    without a Python loader) renders like set_scene with gltf.py's scene of
+    the same file, bit for bit; a file it cannot read is refused with the
+    reason."""
+    from tests.golden import pin_scenes
+    if name == "hand":
+        from tests.test_gltf_c import _document
+        doc, blob = _document(tmp_path)
+        doc = dict(doc, buffers=[{"byteLength": len(blob), "uri": "data:application/octet-stream;base64," +
+                                  base64.b64encode(blob).decode()}])
+        p = str(tmp_path / "hand.gltf")
+        with open(p, "w") as f:
+            json.dump(doc, f)
+        s = io["gltf"].load_scene(p, 48, 32)
+        s.spp, s.max_depth, s.rr_depth = 2, 6, 3
+    else:
+        src = pin_scenes.PIN_SCENES[name]()
+        p = io["gltf"].save_scene(src, str(tmp_path / name))
+        s = loaded_copy(io, src, tmp_path)
+    a = pt.renderer_for(s)
+    a.set_scene_file(p)
+    a.commit()
+    a.render(s.spp)
+    b = pt.renderer_for(s)
+    b.render(s.spp)
+    # textures decode through powf on both sides; where the two loaders'
+    # texels agree exactly (every scene here on one machine) so do the images
+    c = pt.read_gltf(p)
+    exact = all(np.array_equal(x, y) for x, y in zip(c.textures, s.textures))
+    for k in (0, 1, 2, 3):
+        if exact:
+            assert np.array_equal(a.image(k).view(np.uint8), b.image(k).view(np.uint8)), k
+        else:
+            assert np.allclose(a.image(k), b.image(k), rtol=1e-4, atol=1e-5), k
+    bad = tmp_path / "bad.gltf"
+    bad.write_text("{\"asset\": ")
+    with pytest.raises(pt.PTError, match="bad.gltf"):
+        a.set_scene_file(str(bad))
+    a.close()
+    b.close()
