@@ -475,7 +475,7 @@ Image png_read(const std::vector<uint8_t>& buf) {
     default: raise("PNG: unknown colour type " + std::to_string(ctype));
   }
   if (!(depth == 1 || depth == 2 || depth == 4 || depth == 8 || depth == 16)) raise("PNG: bad bit depth");
-  if (W == 0 || H == 0 || (uint64_t)W * H > (1ull << 28)) raise("PNG: bad image size");
+  if (W == 0 || H == 0 || (uint64_t)W * H > (1ull << 26)) raise("PNG: image size 0 or above 2^26 pixels");
   const int bits = depth * nch;
   const size_t stride = ((size_t)W * bits + 7) / 8;
   const size_t bpp = std::max(1, bits / 8);
@@ -674,15 +674,20 @@ class Doc {
     const long long count_ll = as_i(&need(a, "count"), 0, "count");
     if (count_ll < 0 || count_ll > (1LL << 31)) raise("bad accessor count");
     const size_t count = (size_t)count_ll, item = isz * nc;
-    std::vector<double> out(count * nc, 0.0);
     const Json* bv = a.get("bufferView");
-    if (!bv) return out;
+    if (!bv) {  // all zeros; bounded like the largest accessor a buffer could hold
+      if (count * nc > (1ull << 28)) raise("accessor " + std::to_string(ai) + " is too large");
+      return std::vector<double>(count * nc, 0.0);
+    }
     const auto vb = view_bytes(as_i(bv, 0, "bufferView"));
     const std::vector<uint8_t>& raw = vb.first;
     const size_t stride = vb.second ? vb.second : item;
     const size_t off = (size_t)std::max(0LL, as_i(a.get("byteOffset"), 0, "byteOffset"));
-    if (count && off + (count - 1) * stride + item > raw.size()) raise("accessor " + std::to_string(ai) +
-                                                                     " reads past its buffer view");
+    // checked before anything is allocated
+    if (count && (off > raw.size() || (count - 1) > (raw.size() - off) / stride ||
+                  off + (count - 1) * stride + item > raw.size()))
+      raise("accessor " + std::to_string(ai) + " reads past its buffer view");
+    std::vector<double> out(count * nc, 0.0);
     const bool normalized = a.get("normalized") && a.get("normalized")->truthy() && ct != 5126;
     for (size_t i = 0; i < count; ++i) {
       const uint8_t* p = raw.data() + off + i * stride;
@@ -739,6 +744,7 @@ Mat4 node_matrix(const Json& n) {
 // (node index, world matrix) of every node of the default scene, pre-order
 void walk(const Json& j, long long i, const Mat4& parent, std::vector<std::pair<long long, Mat4>>& out, int depth) {
   if (depth > 1024) raise("node hierarchy too deep (a cycle?)");
+  if (out.size() >= (1u << 20)) raise("more than 2^20 node instances (shared subtrees?)");
   const Json& n = at(need(j, "nodes"), i, "nodes");
   const Mat4 M = mul(parent, node_matrix(n));
   out.emplace_back(i, M);

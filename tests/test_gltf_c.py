@@ -297,3 +297,41 @@ def test_malformed_files_are_refused_with_a_reason(pt, lib, tmp_path):
             p.write_text(text)
         st, why = load(p)
         assert st == abi.PT_ERR_INVALID_ARG and name.split(".")[0] in why and len(why) > len(str(p)) + 2, (name, why)
+
+
+def test_mutated_documents_are_read_or_refused(pt, lib, tmp_path):
+    """Seeded byte mutations of the hand-written document (JSON syntax,
+    numbers, indices, base64 of the buffers and PNGs): every one is either
+    read or refused with PT_ERR_INVALID_ARG and a reason, never a crash."""
+    import ctypes as C
+    import random
+    abi = importlib.import_module("hala-pathtracer_gb300.abi")
+    doc, blob = _document(tmp_path)
+    text = json.dumps(dict(doc, buffers=[{"byteLength": len(blob), "uri": _uri(blob)}])).encode()
+    rng = random.Random(7)
+    seen = {abi.PT_OK: 0, abi.PT_ERR_INVALID_ARG: 0}
+    p = tmp_path / "m.gltf"
+    for _ in range(400):
+        b = bytearray(text)
+        for _ in range(rng.randint(1, 6)):
+            k = rng.randrange(len(b))
+            op = rng.random()
+            if op < 0.4:
+                b[k] = rng.randrange(256)
+            elif op < 0.6:
+                del b[k:k + rng.randint(1, 16)]
+            elif op < 0.8:
+                b[k:k] = bytes(rng.choice(b'0123456789-.eE[]{}",:') for _ in range(rng.randint(1, 4)))
+            else:
+                b[k:k] = rng.choice([b"-1", b"99999999999", b"1e308", b"4294967295", b"2147483648"])
+        p.write_bytes(bytes(b))
+        h = C.c_void_p()
+        err = C.create_string_buffer(512)
+        st = lib.pt_gltf_load(str(p).encode(), C.byref(h), err, 512)
+        assert st in seen, st
+        seen[st] += 1
+        if st == abi.PT_OK:
+            lib.pt_gltf_free(h)
+        else:
+            assert not h.value and err.value
+    assert seen[abi.PT_OK] > 0 and seen[abi.PT_ERR_INVALID_ARG] > 0
