@@ -46,6 +46,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
 #include <map>
 #include <memory>
 #include <string>
@@ -1227,6 +1228,9 @@ pt_status pt_gltf_load(const char* path, pt_gltf_scene** out, char* error_messag
   } catch (const std::bad_alloc&) {
     set_error(error_message, error_capacity, "out of host memory");
     return PT_ERR_OOM;
+  } catch (const std::exception& e) {  // nothing may cross the C boundary
+    set_error(error_message, error_capacity, std::string(path) + ": " + e.what());
+    return PT_ERR_INVALID_ARG;
   }
   for (size_t i = 0; i < s->prims.size(); ++i) {
     s->prims[i].vertices = s->verts[i].data();
