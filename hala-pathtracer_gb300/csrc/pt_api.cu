@@ -568,8 +568,10 @@ void pt_material_preprocess(pt_material* m) {
   }
 }
 
-pt_status pt_renderer_create(const pt_tracer_config* cfg, pt_renderer** out) {
+pt_status pt_renderer_create(const pt_tracer_config* cfg, pt_renderer** out) try {
   return renderer_create_with_priority(cfg, 0, out);
+} catch (...) {
+  return host_exception_status(nullptr);
 }
 
 }  // extern "C"
@@ -650,7 +652,7 @@ void pt_renderer_destroy(pt_renderer* r) {
 
 const char* pt_renderer_last_error(const pt_renderer* r) { return r ? r->err.c_str() : "null renderer"; }
 
-pt_status pt_renderer_set_scene(pt_renderer* r, const pt_scene_desc* s) {
+pt_status pt_renderer_set_scene(pt_renderer* r, const pt_scene_desc* s) try {
   if (!r) return PT_ERR_INVALID_ARG;
   AllocScope alloc_scope(r->stream);
   {
@@ -755,9 +757,11 @@ pt_status pt_renderer_set_scene(pt_renderer* r, const pt_scene_desc* s) {
   CK(r, cudaStreamSynchronize(st));
   r->has_scene = true;
   return PT_OK;
+} catch (...) {
+  return host_exception_status(r ? &r->err : nullptr);
 }
 
-pt_status pt_renderer_set_envmap(pt_renderer* r, const float* rgb, uint32_t w, uint32_t h, float rot_deg) {
+pt_status pt_renderer_set_envmap(pt_renderer* r, const float* rgb, uint32_t w, uint32_t h, float rot_deg) try {
   if (!r) return PT_ERR_INVALID_ARG;
   AllocScope alloc_scope(r->stream);
   r->committed = false;
@@ -780,41 +784,53 @@ pt_status pt_renderer_set_envmap(pt_renderer* r, const float* rgb, uint32_t w, u
   // hdri_rotation is given in degrees (conf/*.yaml); the shaders use turns.
   r->env_rotation = rot_deg / 360.0f;
   return PT_OK;
+} catch (...) {
+  return host_exception_status(r ? &r->err : nullptr);
 }
 
-pt_status pt_renderer_set_ground_color(pt_renderer* r, const float rgba[4]) {
+pt_status pt_renderer_set_ground_color(pt_renderer* r, const float rgba[4]) try {
   if (!r || !rgba) return PT_ERR_INVALID_ARG;
   std::memcpy(r->ground, rgba, 16);
   r->view.ground[0] = rgba[0]; r->view.ground[1] = rgba[1]; r->view.ground[2] = rgba[2];
   return PT_OK;
+} catch (...) {
+  return host_exception_status(r ? &r->err : nullptr);
 }
-pt_status pt_renderer_set_sky_color(pt_renderer* r, const float rgba[4]) {
+pt_status pt_renderer_set_sky_color(pt_renderer* r, const float rgba[4]) try {
   if (!r || !rgba) return PT_ERR_INVALID_ARG;
   std::memcpy(r->sky, rgba, 16);
   r->view.sky[0] = rgba[0]; r->view.sky[1] = rgba[1]; r->view.sky[2] = rgba[2];
   return PT_OK;
+} catch (...) {
+  return host_exception_status(r ? &r->err : nullptr);
 }
-pt_status pt_renderer_set_env_intensity(pt_renderer* r, float v) {
+pt_status pt_renderer_set_env_intensity(pt_renderer* r, float v) try {
   if (!r) return PT_ERR_INVALID_ARG;
   r->env_intensity = v;
   r->view.env_intensity = v;
   r->view.env_total_sum = (float)(r->env_total * (double)v);
   return PT_OK;
+} catch (...) {
+  return host_exception_status(r ? &r->err : nullptr);
 }
-pt_status pt_renderer_set_exposure_value(pt_renderer* r, float v) {
+pt_status pt_renderer_set_exposure_value(pt_renderer* r, float v) try {
   if (!r) return PT_ERR_INVALID_ARG;
   r->exposure = v;
   return PT_OK;
+} catch (...) {
+  return host_exception_status(r ? &r->err : nullptr);
 }
-pt_status pt_renderer_set_camera_index(pt_renderer* r, uint32_t i) {
+pt_status pt_renderer_set_camera_index(pt_renderer* r, uint32_t i) try {
   if (!r) return PT_ERR_INVALID_ARG;
   if (r->has_scene && i >= r->cams.size()) return fail(r, PT_ERR_INVALID_ARG, "camera index out of range");
   r->camera_index = i;
   if (r->committed) fill_view(r);
   return PT_OK;
+} catch (...) {
+  return host_exception_status(r ? &r->err : nullptr);
 }
 
-pt_status pt_renderer_commit(pt_renderer* r) {
+pt_status pt_renderer_commit(pt_renderer* r) try {
   if (!r) return PT_ERR_INVALID_ARG;
   AllocScope alloc_scope(r->stream);
   if (!r->has_scene) return fail(r, PT_ERR_STATE, "set_scene must come before commit");
@@ -904,9 +920,11 @@ pt_status pt_renderer_commit(pt_renderer* r) {
   r->stats.features = f;
   r->committed = true;
   return PT_OK;
+} catch (...) {
+  return host_exception_status(r ? &r->err : nullptr);
 }
 
-pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) {
+pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) try {
   if (!r) return PT_ERR_INVALID_ARG;
   AllocScope alloc_scope(r->stream);
   if (!r->committed) return fail(r, PT_ERR_STATE, "commit must come before render");
@@ -1062,9 +1080,11 @@ pt_status pt_renderer_render(pt_renderer* r, uint32_t frames) {
   }
   r->stats.trace_ms = tms;
   return check_traversal(r);
+} catch (...) {
+  return host_exception_status(r ? &r->err : nullptr);
 }
 
-pt_status pt_renderer_set_radiance_cache(pt_renderer* r, const pt_cache_config* cfg) {
+pt_status pt_renderer_set_radiance_cache(pt_renderer* r, const pt_cache_config* cfg) try {
   if (!r) return PT_ERR_INVALID_ARG;
   CK(r, cudaStreamSynchronize(r->stream));
   if (r->cache) pt_cache_destroy(r->cache);
@@ -1097,17 +1117,21 @@ pt_status pt_renderer_set_radiance_cache(pt_renderer* r, const pt_cache_config* 
   r->cache_cfg = c;
   r->cache_on = true;
   return PT_OK;
+} catch (...) {
+  return host_exception_status(r ? &r->err : nullptr);
 }
 
-pt_status pt_renderer_set_profiling(pt_renderer* r, uint32_t flags) {
+pt_status pt_renderer_set_profiling(pt_renderer* r, uint32_t flags) try {
   if (!r) return PT_ERR_INVALID_ARG;
   if (flags & ~(PT_PROFILE_TRACE_TIMING | PT_PROFILE_COUNT | PT_PROFILE_HOST_LOOP))
     return fail(r, PT_ERR_INVALID_ARG, "unknown profiling flag");
   r->profiling = flags;
   return PT_OK;
+} catch (...) {
+  return host_exception_status(r ? &r->err : nullptr);
 }
 
-pt_status pt_renderer_reset(pt_renderer* r) {
+pt_status pt_renderer_reset(pt_renderer* r) try {
   if (!r) return PT_ERR_INVALID_ARG;
   size_t WH = (size_t)r->cfg.width * r->cfg.height;
   CK(r, cudaMemsetAsync(r->accum.p, 0, WH * sizeof(float4), r->stream));
@@ -1118,10 +1142,12 @@ pt_status pt_renderer_reset(pt_renderer* r) {
   r->frame_index = 0;
   r->stats.frame_index = 0;
   return PT_OK;
+} catch (...) {
+  return host_exception_status(r ? &r->err : nullptr);
 }
 
 pt_status pt_renderer_load_accumulation(pt_renderer* r, const float* accum, const float* albedo, const float* normal,
-                                        uint64_t frame_index) {
+                                        uint64_t frame_index) try {
   if (!r) return PT_ERR_INVALID_ARG;
   if (!accum || !albedo || !normal) return fail(r, PT_ERR_INVALID_ARG, "image pointer is null");
   if (r->cfg.max_samples > 0 && frame_index > r->cfg.max_samples)
@@ -1137,9 +1163,11 @@ pt_status pt_renderer_load_accumulation(pt_renderer* r, const float* accum, cons
   r->frame_index = frame_index;
   r->stats.frame_index = frame_index;
   return PT_OK;
+} catch (...) {
+  return host_exception_status(r ? &r->err : nullptr);
 }
 
-pt_status pt_renderer_read_image(pt_renderer* r, pt_image which, void* host, size_t bytes) {
+pt_status pt_renderer_read_image(pt_renderer* r, pt_image which, void* host, size_t bytes) try {
   if (!r) return PT_ERR_INVALID_ARG;
   if (!host) return fail(r, PT_ERR_INVALID_ARG, "host pointer is null");
   const size_t WH = (size_t)r->cfg.width * r->cfg.height;
@@ -1177,9 +1205,11 @@ pt_status pt_renderer_read_image(pt_renderer* r, pt_image which, void* host, siz
       return PT_OK;
   }
   return fail(r, PT_ERR_INVALID_ARG, "unknown image");
+} catch (...) {
+  return host_exception_status(r ? &r->err : nullptr);
 }
 
-pt_status pt_renderer_save_images(pt_renderer* r, const char* prefix) {
+pt_status pt_renderer_save_images(pt_renderer* r, const char* prefix) try {
   if (!r || !prefix) return PT_ERR_INVALID_ARG;
   const uint32_t W = r->cfg.width, H = r->cfg.height;
   const size_t WH = (size_t)W * H;
@@ -1202,28 +1232,36 @@ pt_status pt_renderer_save_images(pt_renderer* r, const char* prefix) {
   for (size_t i = 0; i < WH; ++i) std::fwrite(&rgba[4 * i], 1, 3, f);
   std::fclose(f);
   return PT_OK;
+} catch (...) {
+  return host_exception_status(r ? &r->err : nullptr);
 }
 
-pt_status pt_renderer_wait_idle(pt_renderer* r) {
+pt_status pt_renderer_wait_idle(pt_renderer* r) try {
   if (!r) return PT_ERR_INVALID_ARG;
   CK(r, cudaStreamSynchronize(r->stream));
   return PT_OK;
+} catch (...) {
+  return host_exception_status(r ? &r->err : nullptr);
 }
 
-pt_status pt_renderer_get_stats(const pt_renderer* r, pt_stats* out) {
+pt_status pt_renderer_get_stats(const pt_renderer* r, pt_stats* out) try {
   if (!r || !out) return PT_ERR_INVALID_ARG;
   *out = r->stats;
   return PT_OK;
+} catch (...) {
+  return host_exception_status(nullptr);
 }
 
-pt_status pt_renderer_get_stream(const pt_renderer* r, void** stream) {
+pt_status pt_renderer_get_stream(const pt_renderer* r, void** stream) try {
   if (!r || !stream) return PT_ERR_INVALID_ARG;
   *stream = (void*)r->stream;
   return PT_OK;
+} catch (...) {
+  return host_exception_status(nullptr);
 }
 
 pt_status pt_renderer_trace_rays(pt_renderer* r, const float* rays, uint32_t n, int32_t any_hit, int32_t brute,
-                                 uint32_t* hits) {
+                                 uint32_t* hits) try {
   if (!r) return PT_ERR_INVALID_ARG;
   AllocScope alloc_scope(r->stream);
   if (!r->committed) return fail(r, PT_ERR_STATE, "commit must come before trace_rays");
@@ -1240,22 +1278,28 @@ pt_status pt_renderer_trace_rays(pt_renderer* r, const float* rays, uint32_t n, 
   CK(r, cudaMemcpyAsync(hits, dh.p, 16 * (size_t)n, cudaMemcpyDeviceToHost, r->stream));
   CK(r, cudaStreamSynchronize(r->stream));
   return check_traversal(r);
+} catch (...) {
+  return host_exception_status(r ? &r->err : nullptr);
 }
 
-pt_status pt_renderer_set_bvh_build(pt_renderer* r, uint32_t mode) {
+pt_status pt_renderer_set_bvh_build(pt_renderer* r, uint32_t mode) try {
   if (!r) return PT_ERR_INVALID_ARG;
   if (mode != PT_BVH_BUILD_SAH && mode != PT_BVH_BUILD_FAST) return fail(r, PT_ERR_INVALID_ARG, "unknown BVH build");
   r->bvh_build = mode;
   return PT_OK;
+} catch (...) {
+  return host_exception_status(r ? &r->err : nullptr);
 }
 
-pt_status pt_renderer_set_tail_paths(pt_renderer* r, uint32_t paths) {
+pt_status pt_renderer_set_tail_paths(pt_renderer* r, uint32_t paths) try {
   if (!r) return PT_ERR_INVALID_ARG;
   r->tail_paths = paths;
   return PT_OK;
+} catch (...) {
+  return host_exception_status(r ? &r->err : nullptr);
 }
 
-pt_status pt_renderer_set_traversal_limits(pt_renderer* r, uint32_t stack_entries, uint32_t max_visits) {
+pt_status pt_renderer_set_traversal_limits(pt_renderer* r, uint32_t stack_entries, uint32_t max_visits) try {
   if (!r) return PT_ERR_INVALID_ARG;
   if (stack_entries > 96) return fail(r, PT_ERR_INVALID_ARG, "the traversal stack holds at most 96 entries");
   r->trav_stack = stack_entries ? stack_entries : 96;
@@ -1263,10 +1307,12 @@ pt_status pt_renderer_set_traversal_limits(pt_renderer* r, uint32_t stack_entrie
   r->view.trav_stack = r->trav_stack;
   r->view.trav_visits = r->trav_visits;
   return PT_OK;
+} catch (...) {
+  return host_exception_status(r ? &r->err : nullptr);
 }
 
 pt_status pt_renderer_read_samples(pt_renderer* r, const uint64_t* paths, uint32_t n, float* radiance,
-                                   uint32_t* hash) {
+                                   uint32_t* hash) try {
   if (!r) return PT_ERR_INVALID_ARG;
   AllocScope alloc_scope(r->stream);
   if (!r->cfg.keep_samples) return fail(r, PT_ERR_STATE, "keep_samples is off");
@@ -1294,6 +1340,8 @@ pt_status pt_renderer_read_samples(pt_renderer* r, const uint64_t* paths, uint32
       radiance[3 * i + 2] = tmp[i].z;
     }
   return PT_OK;
+} catch (...) {
+  return host_exception_status(r ? &r->err : nullptr);
 }
 
 }  // extern "C"

@@ -814,7 +814,7 @@ void pt_cache_config_default(pt_cache_config* c) {
   c->min_roughness = 0.3f;
 }
 
-pt_status pt_cache_create(const pt_cache_config* cfg, pt_cache** out) {
+pt_status pt_cache_create(const pt_cache_config* cfg, pt_cache** out) try {
   if (!out) return PT_ERR_INVALID_ARG;
   *out = nullptr;
   pt_cache_config c;
@@ -904,6 +904,8 @@ pt_status pt_cache_create(const pt_cache_config* cfg, pt_cache** out) {
   k->V.grid_grad = reinterpret_cast<float2*>(k->ggrad.p);
   *out = k;
   return PT_OK;
+} catch (...) {
+  return host_exception_status(nullptr);
 }
 
 void pt_cache_destroy(pt_cache* c) {
@@ -917,7 +919,7 @@ void pt_cache_destroy(pt_cache* c) {
 
 const char* pt_cache_last_error(const pt_cache* c) { return c ? c->err.c_str() : "null cache"; }
 
-pt_status pt_cache_set_bounds(pt_cache* c, const float lo[3], const float hi[3]) {
+pt_status pt_cache_set_bounds(pt_cache* c, const float lo[3], const float hi[3]) try {
   if (!c || !lo || !hi) return PT_ERR_INVALID_ARG;
   for (int i = 0; i < 3; ++i) {
     if (!(hi[i] > lo[i])) return cfail(c, PT_ERR_INVALID_ARG, "bounds must have positive extent");
@@ -925,24 +927,30 @@ pt_status pt_cache_set_bounds(pt_cache* c, const float lo[3], const float hi[3])
     c->V.inv_ext[i] = 1.0f / (hi[i] - lo[i]);
   }
   return PT_OK;
+} catch (...) {
+  return host_exception_status(c ? &c->err : nullptr);
 }
 
-pt_status pt_cache_num_params(const pt_cache* c, uint64_t* mlp, uint64_t* grid) {
+pt_status pt_cache_num_params(const pt_cache* c, uint64_t* mlp, uint64_t* grid) try {
   if (!c) return PT_ERR_INVALID_ARG;
   if (mlp) *mlp = NC_PARAMS;
   if (grid) *grid = c->grid_count;
   return PT_OK;
+} catch (...) {
+  return host_exception_status(nullptr);
 }
 
-pt_status pt_cache_get_params(pt_cache* c, float* mlp, float* grid) {
+pt_status pt_cache_get_params(pt_cache* c, float* mlp, float* grid) try {
   if (!c) return PT_ERR_INVALID_ARG;
   CCK(c, cudaStreamSynchronize(c->stream));
   if (mlp) CCK(c, cudaMemcpy(mlp, c->w.p, NC_PARAMS * sizeof(float), cudaMemcpyDeviceToHost));
   if (grid) CCK(c, cudaMemcpy(grid, c->gw.p, c->grid_count * sizeof(float), cudaMemcpyDeviceToHost));
   return PT_OK;
+} catch (...) {
+  return host_exception_status(c ? &c->err : nullptr);
 }
 
-pt_status pt_cache_set_params(pt_cache* c, const float* mlp, const float* grid) {
+pt_status pt_cache_set_params(pt_cache* c, const float* mlp, const float* grid) try {
   if (!c) return PT_ERR_INVALID_ARG;
   cudaStream_t st = c->stream;
   if (mlp) {
@@ -956,6 +964,8 @@ pt_status pt_cache_set_params(pt_cache* c, const float* mlp, const float* grid) 
   CCK(c, cudaGetLastError());
   CCK(c, cudaStreamSynchronize(st));
   return PT_OK;
+} catch (...) {
+  return host_exception_status(c ? &c->err : nullptr);
 }
 
 static pt_status upload_rows(pt_cache* c, const float* records, const float* targets, uint32_t n) {
@@ -972,7 +982,7 @@ static pt_status upload_rows(pt_cache* c, const float* records, const float* tar
   return PT_OK;
 }
 
-pt_status pt_cache_infer(pt_cache* c, const float* records, uint32_t n, float* out_rgb) {
+pt_status pt_cache_infer(pt_cache* c, const float* records, uint32_t n, float* out_rgb) try {
   if (!c) return PT_ERR_INVALID_ARG;
   if (n == 0) return PT_OK;
   if (!records || !out_rgb) return cfail(c, PT_ERR_INVALID_ARG, "null buffer");
@@ -991,10 +1001,12 @@ pt_status pt_cache_infer(pt_cache* c, const float* records, uint32_t n, float* o
     out_rgb[3 * i + 2] = h[i].z;
   }
   return PT_OK;
+} catch (...) {
+  return host_exception_status(c ? &c->err : nullptr);
 }
 
 pt_status pt_cache_gradients(pt_cache* c, const float* records, const float* targets, uint32_t n, float* mlp_grad,
-                             float* grid_grad, float* loss) {
+                             float* grid_grad, float* loss) try {
   if (!c) return PT_ERR_INVALID_ARG;
   if (n == 0 || !records || !targets) return cfail(c, PT_ERR_INVALID_ARG, "empty batch or null buffer");
   pt_status s = upload_rows(c, records, targets, n);
@@ -1018,10 +1030,12 @@ pt_status pt_cache_gradients(pt_cache* c, const float* records, const float* tar
   CCK(c, cudaStreamSynchronize(st));
   CCK(c, tc_status(c));
   return PT_OK;
+} catch (...) {
+  return host_exception_status(c ? &c->err : nullptr);
 }
 
 
-pt_status pt_cache_benchmark(pt_cache* c, uint32_t n, uint32_t iterations, double* infer_ms, double* train_ms) {
+pt_status pt_cache_benchmark(pt_cache* c, uint32_t n, uint32_t iterations, double* infer_ms, double* train_ms) try {
   if (!c || n == 0 || iterations == 0) return PT_ERR_INVALID_ARG;
   cudaStream_t st = c->stream;
   Buf<float4> rec, tgt, out;
@@ -1065,10 +1079,12 @@ pt_status pt_cache_benchmark(pt_cache* c, uint32_t n, uint32_t iterations, doubl
   CCK(c, cudaGetLastError());
   CCK(c, tc_status(c));
   return PT_OK;
+} catch (...) {
+  return host_exception_status(c ? &c->err : nullptr);
 }
 
 pt_status pt_cache_train(pt_cache* c, const float* records, const float* targets, uint32_t n, uint32_t steps,
-                         float* last_loss) {
+                         float* last_loss) try {
   if (!c) return PT_ERR_INVALID_ARG;
   if (n == 0 || !records || !targets) return cfail(c, PT_ERR_INVALID_ARG, "empty batch or null buffer");
   pt_status s = upload_rows(c, records, targets, n);
@@ -1089,6 +1105,8 @@ pt_status pt_cache_train(pt_cache* c, const float* records, const float* targets
   CCK(c, cudaStreamSynchronize(st));
   CCK(c, tc_status(c));
   return PT_OK;
+} catch (...) {
+  return host_exception_status(c ? &c->err : nullptr);
 }
 
 }  // extern "C"

@@ -456,7 +456,7 @@ bool inflate_zlib(const uint8_t* data, size_t size, std::vector<uint8_t>& out, s
 extern "C" {
 
 pt_status pt_exr_read_rgb(const char* path, float* rgb, size_t capacity_floats, uint32_t* width, uint32_t* height,
-                          char* error_message, size_t error_capacity) {
+                          char* error_message, size_t error_capacity) try {
   if (error_message && error_capacity) error_message[0] = '\0';
   if (!path || !width || !height) {
     put_error(error_message, error_capacity, "path, width and height must not be null");
@@ -478,9 +478,14 @@ pt_status pt_exr_read_rgb(const char* path, float* rgb, size_t capacity_floats, 
   }
   std::memcpy(rgb, px.data(), px.size() * sizeof(float));
   return PT_OK;
+} catch (...) {
+  std::string why;
+  const pt_status st = host_exception_status(&why);
+  put_error(error_message, error_capacity, why);
+  return st;
 }
 
-pt_status pt_renderer_set_envmap_file(pt_renderer* r, const char* path, float rotation_degrees) {
+pt_status pt_renderer_set_envmap_file(pt_renderer* r, const char* path, float rotation_degrees) try {
   if (!r) return PT_ERR_INVALID_ARG;
   std::vector<float> px;
   uint32_t W = 0, H = 0;
@@ -491,6 +496,8 @@ pt_status pt_renderer_set_envmap_file(pt_renderer* r, const char* path, float ro
     return PT_ERR_INVALID_ARG;
   }
   return pt_renderer_set_envmap(r, px.data(), W, H, rotation_degrees);
+} catch (...) {
+  return host_exception_status(r ? &r->err : nullptr);
 }
 
 }  // extern "C"

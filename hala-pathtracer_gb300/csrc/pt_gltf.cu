@@ -1259,7 +1259,7 @@ uint32_t pt_gltf_skipped_images(const pt_gltf_scene* scene) { return scene ? sce
 
 void pt_gltf_free(pt_gltf_scene* scene) { delete scene; }
 
-pt_status pt_renderer_set_scene_file(pt_renderer* r, const char* path) {
+pt_status pt_renderer_set_scene_file(pt_renderer* r, const char* path) try {
   if (!r) return PT_ERR_INVALID_ARG;
   char why[512];
   pt_gltf_scene* scene = nullptr;
@@ -1271,6 +1271,8 @@ pt_status pt_renderer_set_scene_file(pt_renderer* r, const char* path) {
   const pt_status rs = pt_renderer_set_scene(r, &scene->desc);
   pt_gltf_free(scene);
   return rs;
+} catch (...) {
+  return host_exception_status(r ? &r->err : nullptr);
 }
 
 }  // extern "C"

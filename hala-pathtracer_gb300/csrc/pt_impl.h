@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <exception>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -234,3 +236,31 @@ pt_status validate_tracer_config(const pt_tracer_config* config, std::string* wh
 uint64_t renderer_estimate_bytes(const pt_scene_desc* desc, uint32_t width, uint32_t height, uint32_t env_w,
                                  uint32_t env_h);
 }  // namespace hpt
+
+// The C entry points are function-try-blocks whose handler returns this:
+// PT_ERR_OOM for a host allocation failure (std::bad_alloc), otherwise
+// PT_ERR_INVALID_ARG, with the exception's text left in *err (the handle's
+// last-error string) when there is one. No C++ exception unwinds into a C
+// caller. Call it only from a catch handler.
+inline pt_status host_exception_status(std::string* err) noexcept {
+  auto note = [err](const char* m) noexcept {
+    if (!err) return;
+    try {
+      *err = m;
+    } catch (...) {
+    }
+  };
+  try {
+    throw;
+  } catch (const std::bad_alloc&) {
+    note("out of host memory");
+    return PT_ERR_OOM;
+  } catch (const std::exception& e) {
+    note(e.what());
+    return PT_ERR_INVALID_ARG;
+  } catch (...) {
+    note("unexpected C++ exception");
+    return PT_ERR_INVALID_ARG;
+  }
+}
+

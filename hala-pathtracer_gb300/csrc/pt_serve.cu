@@ -574,9 +574,25 @@ JobPtr find_job(pt_server* s, uint64_t id) {
 
 }  // namespace
 
+// host_exception_status for the server handle, whose last-error text is
+// guarded by its mutex (an exception thrown under the lock has released it).
+static pt_status server_exception_status(const pt_server* s) noexcept {
+  std::string why;
+  const pt_status st = host_exception_status(&why);
+  if (s) {
+    try {
+      pt_server* m = const_cast<pt_server*>(s);
+      std::lock_guard<std::mutex> g(m->mu);
+      m->err = why;
+    } catch (...) {
+    }
+  }
+  return st;
+}
+
 extern "C" {
 
-pt_status pt_server_create(const pt_server_config* cfg, pt_server** out) {
+pt_status pt_server_create(const pt_server_config* cfg, pt_server** out) try {
   if (!out) return PT_ERR_INVALID_ARG;
   *out = nullptr;
   int ndev = 0;
@@ -607,6 +623,8 @@ pt_status pt_server_create(const pt_server_config* cfg, pt_server** out) {
   s->render_thr = std::thread(render_loop, s);
   *out = s;
   return PT_OK;
+} catch (...) {
+  return host_exception_status(nullptr);
 }
 
 void pt_server_destroy(pt_server* s) {
@@ -640,7 +658,7 @@ const char* pt_server_last_error(const pt_server* s) {
   return copy.c_str();
 }
 
-pt_status pt_server_submit(pt_server* s, const pt_job_desc* jd, uint64_t* job_id) {
+pt_status pt_server_submit(pt_server* s, const pt_job_desc* jd, uint64_t* job_id) try {
   if (!s || !jd || !job_id) return PT_ERR_INVALID_ARG;
   std::string why;
   pt_status v = validate_scene_desc(jd->scene, &why);
@@ -702,9 +720,11 @@ pt_status pt_server_submit(pt_server* s, const pt_job_desc* jd, uint64_t* job_id
   *job_id = j->id;
   s->cv_admit.notify_all();
   return PT_OK;
+} catch (...) {
+  return server_exception_status(s);
 }
 
-pt_status pt_server_poll(pt_server* s, uint64_t id, pt_job_info* info) {
+pt_status pt_server_poll(pt_server* s, uint64_t id, pt_job_info* info) try {
   if (!s || !info) return PT_ERR_INVALID_ARG;
   std::lock_guard<std::mutex> g(s->mu);
   JobPtr j = find_job(s, id);
@@ -724,9 +744,11 @@ pt_status pt_server_poll(pt_server* s, uint64_t id, pt_job_info* info) {
   info->done_ms = j->t_done;
   std::strncpy(info->error, j->err.c_str(), sizeof(info->error) - 1);
   return PT_OK;
+} catch (...) {
+  return server_exception_status(s);
 }
 
-pt_status pt_server_wait(pt_server* s, uint64_t id, uint32_t timeout_ms) {
+pt_status pt_server_wait(pt_server* s, uint64_t id, uint32_t timeout_ms) try {
   if (!s) return PT_ERR_INVALID_ARG;
   std::unique_lock<std::mutex> lk(s->mu);
   JobPtr j = find_job(s, id);
@@ -741,9 +763,11 @@ pt_status pt_server_wait(pt_server* s, uint64_t id, uint32_t timeout_ms) {
   }
   if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred)) return PT_ERR_TIMEOUT;
   return PT_OK;
+} catch (...) {
+  return server_exception_status(s);
 }
 
-pt_status pt_server_read_image(pt_server* s, uint64_t id, pt_image which, void* host, size_t bytes) {
+pt_status pt_server_read_image(pt_server* s, uint64_t id, pt_image which, void* host, size_t bytes) try {
   if (!s) return PT_ERR_INVALID_ARG;
   JobPtr j;
   {
@@ -767,9 +791,11 @@ pt_status pt_server_read_image(pt_server* s, uint64_t id, pt_image which, void* 
   pt_status ps = pt_renderer_read_image(j->r, which, host, bytes);
   if (ps != PT_OK) return srv_fail(s, ps, pt_renderer_last_error(j->r));
   return PT_OK;
+} catch (...) {
+  return server_exception_status(s);
 }
 
-pt_status pt_server_cancel(pt_server* s, uint64_t id) {
+pt_status pt_server_cancel(pt_server* s, uint64_t id) try {
   if (!s) return PT_ERR_INVALID_ARG;
   std::lock_guard<std::mutex> g(s->mu);
   JobPtr j = find_job(s, id);
@@ -789,9 +815,11 @@ pt_status pt_server_cancel(pt_server* s, uint64_t id) {
   s->cv_admit.notify_all();
   s->cv_render.notify_all();
   return PT_OK;
+} catch (...) {
+  return server_exception_status(s);
 }
 
-pt_status pt_server_release(pt_server* s, uint64_t id) {
+pt_status pt_server_release(pt_server* s, uint64_t id) try {
   if (!s) return PT_ERR_INVALID_ARG;
   JobPtr j;
   {
@@ -820,17 +848,21 @@ pt_status pt_server_release(pt_server* s, uint64_t id) {
   }
   destroy_renderer(j);
   return PT_OK;
+} catch (...) {
+  return server_exception_status(s);
 }
 
-pt_status pt_server_pause(pt_server* s, int32_t paused) {
+pt_status pt_server_pause(pt_server* s, int32_t paused) try {
   if (!s) return PT_ERR_INVALID_ARG;
   std::lock_guard<std::mutex> g(s->mu);
   s->paused = paused != 0;
   s->cv_render.notify_all();
   return PT_OK;
+} catch (...) {
+  return server_exception_status(s);
 }
 
-pt_status pt_server_get_stats(pt_server* s, pt_server_stats* out) {
+pt_status pt_server_get_stats(pt_server* s, pt_server_stats* out) try {
   if (!s || !out) return PT_ERR_INVALID_ARG;
   std::lock_guard<std::mutex> g(s->mu);
   *out = s->st;
@@ -839,6 +871,8 @@ pt_status pt_server_get_stats(pt_server* s, pt_server_stats* out) {
   out->resident_bytes = s->resident;
   out->uptime_ms = s->now_ms();
   return PT_OK;
+} catch (...) {
+  return server_exception_status(s);
 }
 
 }  // extern "C"
