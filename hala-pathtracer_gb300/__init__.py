@@ -110,6 +110,22 @@ class Renderer:
         library itself (pt_renderer_set_scene_file)."""
         self._check(self._lib.pt_renderer_set_scene_file(self._h, str(path).encode()))
 
+    def load_blue_noise_texture(self, path):
+        """HalaRenderer::load_blue_noise_texture: the camera jitter's RGBA8
+        texture from an 8-bit PNG (None: the substitute table)."""
+        self._check(self._lib.pt_renderer_load_blue_noise_texture(self._h, None if path is None else
+                                                                   str(path).encode()))
+
+    def set_blue_noise(self, rgba8):
+        """The same texture from (1024, 1024, 4) uint8 texels (None: the substitute)."""
+        if rgba8 is None:
+            self._check(self._lib.pt_renderer_set_blue_noise(self._h, None))
+            return
+        a = np.ascontiguousarray(rgba8, np.uint8)
+        if a.shape != (abi.PT_BLUE_NOISE_SIZE, abi.PT_BLUE_NOISE_SIZE, 4):
+            raise ValueError(f"blue-noise texels must be ({abi.PT_BLUE_NOISE_SIZE}, {abi.PT_BLUE_NOISE_SIZE}, 4)")
+        self._check(self._lib.pt_renderer_set_blue_noise(self._h, a.ctypes.data))
+
     def set_ground_color(self, rgba):
         self._check(self._lib.pt_renderer_set_ground_color(self._h, _f4(rgba)))
 
@@ -247,6 +263,8 @@ def renderer_for(scene, bvh_build=None, **cfg_over):
     if bvh_build is not None:
         r.set_bvh_build(bvh_build)
     r.set_scene(scene)
+    if getattr(scene, "blue_noise", None) is not None:
+        r.set_blue_noise(scene.blue_noise)
     if scene.env_rgb is not None:
         r.set_envmap(scene.env_rgb, scene.env_rotation_deg)
     else:
@@ -289,6 +307,22 @@ def read_gltf(path):
         return s
     finally:
         lib.pt_gltf_free(h)
+
+
+def read_png_rgba8(path):
+    """(H, W, 4) uint8 texels of an 8-bit PNG through the library's own
+    reader (pt_png_read_rgba8)."""
+    lib = load_library()
+    w, h = C.c_uint32(), C.c_uint32()
+    err = C.create_string_buffer(256)
+    st = lib.pt_png_read_rgba8(str(path).encode(), None, 0, C.byref(w), C.byref(h), err, 256)
+    if st != abi.PT_OK:
+        raise PTError(st, err.value.decode())
+    out = np.empty((h.value, w.value, 4), np.uint8)
+    st = lib.pt_png_read_rgba8(str(path).encode(), out.ctypes.data, out.size, C.byref(w), C.byref(h), err, 256)
+    if st != abi.PT_OK:
+        raise PTError(st, err.value.decode())
+    return out
 
 
 def read_exr(path):

@@ -25,6 +25,7 @@ STATUS_NAMES = {
 PT_MAX_CAMERAS = 8
 PT_MAX_LIGHTS = 16
 PT_INVALID_INDEX = 0xFFFFFFFF
+PT_BLUE_NOISE_SIZE = 1024
 
 LIGHT_POINT, LIGHT_DIRECTIONAL, LIGHT_SPOT, LIGHT_QUAD, LIGHT_SPHERE = 0, 1, 2, 3, 4
 MEDIUM_NONE, MEDIUM_ABSORB, MEDIUM_SCATTER, MEDIUM_EMISSIVE = 0, 1, 2, 3
@@ -190,6 +191,10 @@ RENDERER_SIGNATURES = {
                                          C.c_uint32, C.c_float]),
     "pt_renderer_set_envmap_file": (C.c_int, [C.c_void_p, C.c_char_p, C.c_float]),
     "pt_renderer_set_scene_file": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "pt_renderer_load_blue_noise_texture": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "pt_renderer_set_blue_noise": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "pt_png_read_rgba8": (C.c_int, [C.c_char_p, C.c_void_p, C.c_size_t, C.POINTER(C.c_uint32),
+                                    C.POINTER(C.c_uint32), C.c_char_p, C.c_size_t]),
     "pt_gltf_load": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p), C.c_char_p, C.c_size_t]),
     "pt_gltf_scene_desc": (C.POINTER(SceneDesc), [C.c_void_p]),
     "pt_gltf_skipped_images": (C.c_uint32, [C.c_void_p]),

@@ -410,6 +410,7 @@ void fill_view(pt_renderer* r) {
   S.trav_stack = r->trav_stack;
   S.trav_visits = r->trav_visits;
   S.err = r->errw.p;
+  S.blue_noise = r->has_blue_noise ? r->blue_noise.p : nullptr;
 }
 
 // Reads and clears the traversal error word (stream-ordered; synchronises).
@@ -820,6 +821,24 @@ pt_status pt_renderer_set_exposure_value(pt_renderer* r, float v) try {
 } catch (...) {
   return host_exception_status(r ? &r->err : nullptr);
 }
+pt_status pt_renderer_set_blue_noise(pt_renderer* r, const uint8_t* rgba8) try {
+  if (!r) return PT_ERR_INVALID_ARG;
+  if (!rgba8) {
+    r->has_blue_noise = false;
+  } else {
+    AllocScope alloc_scope(r->stream);
+    const size_t n = (size_t)PT_BLUE_NOISE_SIZE * PT_BLUE_NOISE_SIZE;
+    CK(r, r->blue_noise.ensure(n));
+    CK(r, cudaMemcpyAsync(r->blue_noise.p, rgba8, n * sizeof(uchar4), cudaMemcpyHostToDevice, r->stream));
+    CK(r, cudaStreamSynchronize(r->stream));
+    r->has_blue_noise = true;
+  }
+  if (r->committed) fill_view(r);
+  return PT_OK;
+} catch (...) {
+  return host_exception_status(r ? &r->err : nullptr);
+}
+
 pt_status pt_renderer_set_camera_index(pt_renderer* r, uint32_t i) try {
   if (!r) return PT_ERR_INVALID_ARG;
   if (r->has_scene && i >= r->cams.size()) return fail(r, PT_ERR_INVALID_ARG, "camera index out of range");

@@ -242,11 +242,16 @@ __device__ __forceinline__ float4 blue_noise_texel(uint32_t x, uint32_t y) {
   return make_float4((float)(v.x >> 24) / 255.0f, (float)(v.y >> 24) / 255.0f,
                      (float)(v.z >> 24) / 255.0f, (float)(v.w >> 24) / 255.0f);
 }
-// shift2 + rand4blue, wltcRS.glsl:43-53
-__device__ __forceinline__ float4 rand4blue(uint4& s1, int px, int py) {
+// shift2 + rand4blue, wltcRS.glsl:43-53: texelFetch of the loaded RGBA8
+// texture (UNORM: byte / 255), or the substitute when none is loaded
+__device__ __forceinline__ float4 rand4blue(uint4& s1, int px, int py, const uchar4* tex) {
   pcg4d(s1);
   int sx = (px + (int)(s1.x % 0x0fffffffu)) % 1024;
   int sy = (py + (int)(s1.y % 0x0fffffffu)) % 1024;
+  if (tex) {
+    const uchar4 t = tex[(uint32_t)sy * 1024u + (uint32_t)sx];
+    return make_float4((float)t.x / 255.0f, (float)t.y / 255.0f, (float)t.z / 255.0f, (float)t.w / 255.0f);
+  }
   return blue_noise_texel((uint32_t)sx, (uint32_t)sy);
 }
 

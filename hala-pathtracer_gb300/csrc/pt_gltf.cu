@@ -419,138 +419,19 @@ std::vector<uint8_t> uri_bytes(const std::string& uri, const std::string& base) 
   return read_file(base.empty() ? rel : base + "/" + rel);
 }
 
-// ------------------------------------------------------------------ PNG
-// Non-interlaced PNG of every colour type at bit depths 1-16 with the five
-// scanline filters, to float RGBA in [0, 1] (the Python png.read).
+// ------------------------------------------------------------------ images
 const uint8_t PNG_SIG[8] = {0x89, 'P', 'N', 'G', '\r', '\n', 0x1A, '\n'};
-
-uint32_t be32(const uint8_t* p) { return (uint32_t)p[0] << 24 | (uint32_t)p[1] << 16 | (uint32_t)p[2] << 8 | p[3]; }
 
 struct Image {
   uint32_t w = 0, h = 0;
   std::vector<float> rgba;
 };
 
+// float RGBA in [0, 1], as the Python png.read gives it (pt_png.cu)
 Image png_read(const std::vector<uint8_t>& buf) {
-  if (buf.size() < 8 || std::memcmp(buf.data(), PNG_SIG, 8) != 0) raise("PNG: not a PNG file");
-  size_t pos = 8;
-  std::vector<uint8_t> idat, plte, trns;
-  bool have_hdr = false, have_trns = false;
-  uint32_t W = 0, H = 0;
-  int depth = 0, ctype = 0, interlace = 0;
-  while (pos < buf.size()) {
-    if (pos + 8 > buf.size()) raise("PNG: truncated chunk");
-    const uint32_t n = be32(&buf[pos]);
-    const uint8_t* typ = &buf[pos + 4];
-    if ((size_t)n > buf.size() - pos - 8) raise("PNG: truncated chunk");
-    const uint8_t* data = &buf[pos + 8];
-    pos += 12 + (size_t)n;
-    if (!std::memcmp(typ, "IHDR", 4)) {
-      if (n < 13) raise("PNG: short IHDR");
-      W = be32(data);
-      H = be32(data + 4);
-      depth = data[8];
-      ctype = data[9];
-      interlace = data[12];
-      have_hdr = true;
-    } else if (!std::memcmp(typ, "PLTE", 4)) {
-      plte.assign(data, data + n);
-    } else if (!std::memcmp(typ, "tRNS", 4)) {
-      trns.assign(data, data + n);
-      have_trns = true;
-    } else if (!std::memcmp(typ, "IDAT", 4)) {
-      idat.insert(idat.end(), data, data + n);
-    } else if (!std::memcmp(typ, "IEND", 4)) {
-      break;
-    }
-  }
-  if (!have_hdr) raise("PNG: missing IHDR");
-  if (interlace) raise("PNG: interlaced PNGs are not supported");
-  int nch;
-  switch (ctype) {
-    case 0: nch = 1; break;
-    case 2: nch = 3; break;
-    case 3: nch = 1; break;
-    case 4: nch = 2; break;
-    case 6: nch = 4; break;
-    default: raise("PNG: unknown colour type " + std::to_string(ctype));
-  }
-  if (!(depth == 1 || depth == 2 || depth == 4 || depth == 8 || depth == 16)) raise("PNG: bad bit depth");
-  if (W == 0 || H == 0 || (uint64_t)W * H > (1ull << 26)) raise("PNG: image size 0 or above 2^26 pixels");
-  const int bits = depth * nch;
-  const size_t stride = ((size_t)W * bits + 7) / 8;
-  const size_t bpp = std::max(1, bits / 8);
-  std::vector<uint8_t> raw;
-  const size_t want = (stride + 1) * H;
-  if (!hpt::inflate_zlib(idat.data(), idat.size(), raw, 2 * want + 65536) || raw.size() < want)
-    raise("PNG: corrupt image data");
-  std::vector<uint8_t> rows(stride * H), prev(stride, 0);
-  for (uint32_t y = 0; y < H; ++y) {
-    const uint8_t f = raw[y * (stride + 1)];
-    const uint8_t* in = &raw[y * (stride + 1) + 1];
-    uint8_t* r = &rows[y * stride];
-    for (size_t i = 0; i < stride; ++i) {
-      const int a = i >= bpp ? r[i - bpp] : 0, b = prev[i], c = i >= bpp ? prev[i - bpp] : 0;
-      int pred;
-      switch (f) {
-        case 0: pred = 0; break;
-        case 1: pred = a; break;
-        case 2: pred = b; break;
-        case 3: pred = (a + b) >> 1; break;
-        case 4: {
-          const int pp = a + b - c, pa = std::abs(pp - a), pb = std::abs(pp - b), pc = std::abs(pp - c);
-          pred = (pa <= pb && pa <= pc) ? a : (pb <= pc ? b : c);
-          break;
-        }
-        default: raise("PNG: unknown filter type " + std::to_string(f));
-      }
-      r[i] = (uint8_t)(in[i] + pred);
-    }
-    std::memcpy(prev.data(), r, stride);
-  }
-  // samples as float: 16 and 8 bits divided by 65535 / 255, lower depths
-  // by 2^depth - 1; palette indices stay integers
-  const float maxv = depth == 16 ? 65535.0f : depth == 8 ? 255.0f : (float)((1 << depth) - 1);
-  auto sample = [&](uint32_t y, uint32_t x, int ch) -> float {
-    const uint8_t* r = &rows[y * stride];
-    uint32_t v;
-    if (depth == 16) {
-      const size_t o = ((size_t)x * nch + ch) * 2;
-      v = (uint32_t)r[o] << 8 | r[o + 1];
-    } else if (depth == 8) {
-      v = r[(size_t)x * nch + ch];
-    } else {
-      const size_t bit = ((size_t)x * nch + ch) * depth;
-      v = (r[bit >> 3] >> (8 - depth - (bit & 7))) & ((1u << depth) - 1u);
-    }
-    return ctype == 3 ? (float)v : (float)v / maxv;
-  };
   Image im;
-  im.w = W;
-  im.h = H;
-  im.rgba.resize((size_t)W * H * 4);
-  if (ctype == 3 && plte.size() < 3) raise("PNG: palette image without PLTE");
-  const size_t npal = plte.size() / 3;
-  for (uint32_t y = 0; y < H; ++y)
-    for (uint32_t x = 0; x < W; ++x) {
-      float* o = &im.rgba[((size_t)y * W + x) * 4];
-      if (ctype == 3) {
-        const size_t i = (size_t)sample(y, x, 0);
-        if (i >= npal) raise("PNG: palette index out of range");
-        for (int k = 0; k < 3; ++k) o[k] = (float)plte[3 * i + k] / 255.0f;
-        const uint8_t a = (have_trns && i < trns.size()) ? trns[i] : 255;
-        o[3] = (float)a / 255.0f;
-      } else if (nch == 1) {
-        o[0] = o[1] = o[2] = sample(y, x, 0);
-        o[3] = 1.0f;
-      } else if (nch == 2) {
-        o[0] = o[1] = o[2] = sample(y, x, 0);
-        o[3] = sample(y, x, 1);
-      } else {
-        for (int k = 0; k < nch; ++k) o[k] = sample(y, x, k);
-        if (nch == 3) o[3] = 1.0f;
-      }
-    }
+  const std::string why = hpt::png_decode_float(buf.data(), buf.size(), im.w, im.h, im.rgba);
+  if (!why.empty()) raise("PNG: " + why);
   return im;
 }
 

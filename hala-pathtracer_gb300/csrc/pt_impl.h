@@ -183,6 +183,9 @@ struct pt_renderer {
   double env_total = 1.0;
   hpt::Buf<float4> env;
   hpt::Buf<uint2> alias_rows, alias_cols;
+  // loaded blue-noise texture (load_blue_noise_texture), else the substitute
+  hpt::Buf<uchar4> blue_noise;
+  bool has_blue_noise = false;
 
   hpt::DevScene view{};
   uint32_t features = 0;

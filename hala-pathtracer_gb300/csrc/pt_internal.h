@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <string>
 #include <vector>
 
 #include "pt_types.h"
@@ -27,6 +28,11 @@ int device_sm_count();
 // pt_exr.cu: a zlib stream (RFC 1950/1951) into `out`, at most `limit`
 // bytes; false on any format error (also used for PNG image data).
 bool inflate_zlib(const uint8_t* data, size_t size, std::vector<uint8_t>& out, size_t limit);
+// pt_png.cu: a PNG file's bytes as float RGBA in [0, 1] (every colour type
+// and bit depth) or as RGBA8 (8-bit and palette images); "" on success,
+// otherwise the reason.
+std::string png_decode_float(const uint8_t* data, size_t size, uint32_t& w, uint32_t& h, std::vector<float>& rgba);
+std::string png_decode_rgba8(const uint8_t* data, size_t size, uint32_t& w, uint32_t& h, std::vector<uint8_t>& rgba);
 
 // pt_render.cu
 void launch_camera(const DevScene& S, const PathState& P, uint64_t g0, uint32_t n, uint32_t* q_active,

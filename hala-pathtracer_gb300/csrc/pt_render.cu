@@ -42,7 +42,7 @@ __device__ __forceinline__ void init_path(const DevScene& S, const PathState& P,
   uint32_t sf = frame + S.seed;
   uint4 s0 = rng_seed_s0(px, py, sf);
   uint4 s1 = rng_seed_s1(sf);
-  float4 r = rand4blue(s1, (int)px, (int)py);
+  float4 r = rand4blue(s1, (int)px, (int)py, S.blue_noise);
   const DevCamera& cam = S.cam;
   float r1 = 2.0f * r.x, r2 = 2.0f * r.y;
   float jx = r1 < 1.0f ? sqrtf(r1) - 1.0f : 1.0f - sqrtf(2.0f - r1);

@@ -122,6 +122,9 @@ struct DevScene {
   // device word their violations are reported in (TRAV_ERR_* bits)
   uint32_t trav_stack, trav_visits;
   uint32_t* err;
+  // blue-noise texture of the camera jitter (PT_BLUE_NOISE_SIZE^2 RGBA8
+  // texels), or null for the substitute table
+  const uchar4* blue_noise;
 };
 
 // Structure-of-arrays path state of one wavefront (capacity P paths).

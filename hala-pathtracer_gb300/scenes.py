@@ -370,6 +370,7 @@ class Scene:
         self.spp, self.max_depth, self.rr_depth, self.seed = 16, 8, 0, 0
         self.tonemap = (True, True, False)
         self.textures = []       # (H, W, 4) float32 RGBA, linear values
+        self.blue_noise = None   # (1024, 1024, 4) uint8 camera-jitter texture, or None: the substitute
         self._keep = []
 
     def add_material(self, m):

@@ -34,6 +34,8 @@ extern "C" {
 #define PT_MAX_CAMERAS 8u
 #define PT_MAX_LIGHTS 16u
 #define PT_INVALID_INDEX 0xFFFFFFFFu
+/* side of the blue-noise texture the camera jitter reads (wltcRS.glsl:43-53) */
+#define PT_BLUE_NOISE_SIZE 1024u
 
 /* Light types, constants.glsl:14-18 */
 #define PT_LIGHT_POINT 0
@@ -288,6 +290,22 @@ const pt_scene_desc* pt_gltf_scene_desc(const pt_gltf_scene* scene);
 /* Images the reader left out (not PNG): the maps that named them stay unset. */
 uint32_t pt_gltf_skipped_images(const pt_gltf_scene* scene);
 void pt_gltf_free(pt_gltf_scene* scene);
+/* HalaRenderer::load_blue_noise_texture (src/bin/hala-pathtracer.rs:195): the
+ * RGBA8 texture the camera rays' jitter reads (rand4blue, wltcRS.glsl:43-53:
+ * texel ((pixel + shift) % 1024), channels / 255). An 8-bit or palette PNG of
+ * at least 1024 x 1024; its top-left 1024 x 1024 texels are used. Until one is
+ * loaded, and after a NULL path, a deterministic substitute table is read
+ * (the reference's assets/textures/blue_noise.png is not in its checkout).
+ * Takes effect at the next render; no new commit is needed. */
+pt_status pt_renderer_load_blue_noise_texture(pt_renderer* r, const char* path);
+/* The same with texels the host decoded: PT_BLUE_NOISE_SIZE^2 RGBA8 texels,
+ * row-major, row 0 first; NULL returns to the substitute. */
+pt_status pt_renderer_set_blue_noise(pt_renderer* r, const uint8_t* rgba8);
+/* The PNG reader behind pt_renderer_load_blue_noise_texture: RGBA8 bytes of an
+ * 8-bit or palette PNG (grey and RGB get alpha 255), row 0 at the top. With
+ * rgba = NULL only *width and *height are set. */
+pt_status pt_png_read_rgba8(const char* path, uint8_t* rgba, size_t capacity_bytes, uint32_t* width,
+                            uint32_t* height, char* error_message, size_t error_capacity);
 /* HalaRenderer::set_ground_color / set_sky_color (src/bin/hala-pathtracer.rs:205-206). */
 pt_status pt_renderer_set_ground_color(pt_renderer* r, const float rgba[4]);
 pt_status pt_renderer_set_sky_color(pt_renderer* r, const float rgba[4]);

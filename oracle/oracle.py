@@ -57,6 +57,7 @@ def lib():
             "or_set_env_intensity": (None, [P, C.c_float]),
             "or_set_exposure_value": (None, [P, C.c_float]),
             "or_set_camera_index": (None, [P, C.c_uint32]),
+            "or_set_blue_noise": (None, [P, C.c_void_p]),
             "or_commit": (C.c_int, [P]),
             "or_features": (C.c_uint32, [P]),
             "or_render": (C.c_int, [P, C.c_uint32, C.c_int]),
@@ -135,6 +136,11 @@ class Oracle:
         L.or_set_sky_color(self.h, s)
         L.or_set_env_intensity(self.h, scene.env_intensity)
         L.or_set_exposure_value(self.h, scene.exposure_value)
+        bn = getattr(scene, "blue_noise", None)
+        if bn is not None:
+            self._blue_noise = np.ascontiguousarray(bn, np.uint8)
+            assert self._blue_noise.shape == (1024, 1024, 4)
+            L.or_set_blue_noise(self.h, self._blue_noise.ctypes.data)
         import time
         t0 = time.perf_counter()
         rc = L.or_commit(self.h)

@@ -101,11 +101,17 @@ inline void blue_noise_texel(uint32_t x, uint32_t y, float out[4]) {
   out[3] = (float)(v.w >> 24) / 255.0f;
 }
 
-// shift2 + rand4blue, wltcRS.glsl:43-53
-inline void rand4blue(RNG& r, float out[4]) {
+// shift2 + rand4blue, wltcRS.glsl:43-53: texelFetch of a loaded 1024 x 1024
+// RGBA8 texture (UNORM, byte / 255) when `tex` is given, else the substitute
+inline void rand4blue(RNG& r, const uint8_t* tex, float out[4]) {
   pcg4d(r.s1);
   int sx = (r.px + (int)(r.s1.x % 0x0fffffffu)) % 1024;
   int sy = (r.py + (int)(r.s1.y % 0x0fffffffu)) % 1024;
+  if (tex) {
+    const uint8_t* t = tex + 4 * ((size_t)sy * 1024 + (size_t)sx);
+    for (int k = 0; k < 4; ++k) out[k] = (float)t[k] / 255.0f;
+    return;
+  }
   blue_noise_texel((uint32_t)sx, (uint32_t)sy, out);
 }
 
@@ -345,6 +351,7 @@ struct Ctx {
   std::vector<Camera> cams;
   std::vector<Texture> texs;
   uint32_t camera_index = 0;
+  std::vector<uint8_t> blue_noise;  // 1024 x 1024 RGBA8, or empty: the substitute
   // environment, inc/global.glsl:11-24
   bool env_map = false;
   std::vector<float> env_rgb;
@@ -1516,7 +1523,7 @@ struct Tracer {
   void gen_camera_ray(uint32_t px, uint32_t py) {
     const Camera& cam = c.cams[c.camera_index < c.cams.size() ? c.camera_index : 0];
     float r[4];
-    rand4blue(rng, r);
+    rand4blue(rng, c.blue_noise.empty() ? nullptr : c.blue_noise.data(), r);
     float r1 = 2.0f * r[0], r2 = 2.0f * r[1];
     float jx = r1 < 1.0f ? std::sqrt(r1) - 1.0f : 1.0f - std::sqrt(2.0f - r1);
     float jy = r2 < 1.0f ? std::sqrt(r2) - 1.0f : 1.0f - std::sqrt(2.0f - r2);
@@ -1883,6 +1890,11 @@ void or_set_sky_color(or_ctx* o, const float v[4]) { o->c.sky = V3(v[0], v[1], v
 void or_set_env_intensity(or_ctx* o, float v) { o->c.env_intensity = v; o->c.committed = false; }
 void or_set_exposure_value(or_ctx* o, float v) { o->c.exposure = v; }
 void or_set_camera_index(or_ctx* o, uint32_t i) { o->c.camera_index = i; }
+
+void or_set_blue_noise(or_ctx* o, const uint8_t* rgba8) {
+  if (rgba8) o->c.blue_noise.assign(rgba8, rgba8 + 4 * 1024 * 1024);
+  else o->c.blue_noise.clear();
+}
 
 int or_commit(or_ctx* o) {
   if (!o) return PT_ERR_INVALID_ARG;

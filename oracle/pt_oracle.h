@@ -30,6 +30,9 @@ void or_set_sky_color(or_ctx* c, const float rgba[4]);
 void or_set_env_intensity(or_ctx* c, float v);
 void or_set_exposure_value(or_ctx* c, float v);
 void or_set_camera_index(or_ctx* c, uint32_t i);
+/* The camera jitter's blue-noise texture: 1024 x 1024 RGBA8 texels, row 0
+ * first (load_blue_noise_texture); NULL returns to the substitute table. */
+void or_set_blue_noise(or_ctx* c, const uint8_t* rgba8);
 /* Builds the BVH and the environment alias tables; picks the feature set. */
 int or_commit(or_ctx* c);
 uint32_t or_features(const or_ctx* c);
