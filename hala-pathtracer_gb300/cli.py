@@ -15,6 +15,9 @@ import os
 import sys
 import time
 
+# the texture the reference loads before its scene (src/bin/hala-pathtracer.rs:195)
+BLUE_NOISE = "./assets/textures/blue_noise.png"
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 if ROOT not in sys.path:
@@ -44,6 +47,9 @@ def main(argv=None):
     ap.add_argument("--out", default="", help="image prefix for save_images")
     ap.add_argument("--seed", type=int, default=None)
     ap.add_argument("--wave", type=int, default=0, help="paths per wavefront (0 = library default)")
+    ap.add_argument("--blue-noise", default=None,
+                    help=f"camera-jitter texture (default with -c: {BLUE_NOISE} where it exists, "
+                         "else the built-in substitute)")
     args = ap.parse_args(argv)
     if bool(args.config) == bool(args.workload):
         ap.error("give exactly one of -c/--config or --workload")
@@ -59,6 +65,9 @@ def main(argv=None):
         scene = loader.load_scene(scene_path, cfg.window.width, cfg.window.height)
         env = cfgmod.environment_settings(cfg)
         r = pt.Renderer(cfgmod.tracer_config(cfg, seed=args.seed or 0, wave_paths=args.wave))
+        bn = resolve(args.blue_noise or BLUE_NOISE, base)
+        if args.blue_noise or os.path.exists(bn):
+            r.load_blue_noise_texture(bn)
         r.set_scene(scene)
         if env["hdri_file"]:
             exr = importlib.import_module("hala-pathtracer_gb300.exr")
