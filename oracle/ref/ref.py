@@ -40,6 +40,7 @@ def _lib(perm):
             ("ref_set_envmap", C.c_int, [P, C.POINTER(C.c_float), C.c_uint32, C.c_uint32, C.c_float]),
             ("ref_set_colors", None, [P, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
             ("ref_set_env_intensity", None, [P, C.c_float]),
+            ("ref_set_blue_noise", None, [P, C.c_void_p]),
             ("ref_set_exposure_value", None, [P, C.c_float]),
             ("ref_commit", C.c_int, [P]),
             ("ref_render", C.c_int, [P, C.c_uint32, C.c_int]),
@@ -71,6 +72,10 @@ class RefRenderer:
         self.L.ref_set_colors(self.h, (C.c_float * 4)(*scene.ground_color), (C.c_float * 4)(*scene.sky_color))
         self.L.ref_set_env_intensity(self.h, scene.env_intensity)
         self.L.ref_set_exposure_value(self.h, scene.exposure_value)
+        bn = getattr(scene, "blue_noise", None)
+        if bn is not None:
+            self._blue_noise = np.ascontiguousarray(bn, np.uint8)
+            self.L.ref_set_blue_noise(self.h, self._blue_noise.ctypes.data)
         self.L.ref_commit(self.h)
         self.width, self.height = self.cfg.width, self.cfg.height
 

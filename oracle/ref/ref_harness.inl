@@ -13,8 +13,9 @@
 //     g_ray_payload / g_shadow_ray_payload / g_trans_ray_payload;
 //   * executeCallableEXT: the 15 callables in the SBT order of
 //     src/bin/hala-pathtracer.rs:170-186;
-//   * textures: blue-noise substitute (pcg4d of the texel coordinates read as
-//     RGBA8), nearest-texel environment lookups (u wraps, v clamps), and the
+//   * textures: the blue-noise texture (a loaded 1024 x 1024 RGBA8 table,
+//     else the substitute: pcg4d of the texel coordinates read as RGBA8),
+//     nearest-texel environment lookups (u wraps, v clamps), and the
 //     two distribution textures realised by FP64 alias tables;
 //   * images: the accumulation, albedo, normal and RGBA8 final images.
 #include <atomic>
@@ -79,6 +80,8 @@ struct Ctx {
   std::vector<std::vector<float>> tex_rgba;
   std::vector<uint> tex_w, tex_h;
   std::vector<sampler2D> tex_samplers;
+  // blue-noise texels (1024 x 1024 RGBA8) or empty: the substitute
+  std::vector<unsigned char> blue_noise;
 };
 
 Ctx* g_ctx = nullptr;
@@ -161,7 +164,12 @@ void build_alias(const double* w, uint n, float* prob, uint* alias) {
 
 using namespace refh;
 
-vec4 texelFetch(const texture2D&, const ivec2& p, int) {
+vec4 texelFetch(const texture2D&, const ivec2& p, int) {  // g_blue_noise, the only texelFetch
+  const Ctx& c = *g_ctx;
+  if (!c.blue_noise.empty()) {  // RGBA8 UNORM
+    const unsigned char* t = &c.blue_noise[4 * ((size_t)p.y * 1024 + (size_t)p.x)];
+    return vec4((float)t[0] / 255.0f, (float)t[1] / 255.0f, (float)t[2] / 255.0f, (float)t[3] / 255.0f);
+  }
   uvec4 v = uvec4((uint)p.x, (uint)p.y, 0x2545F491u, 0x9E3779B9u);
   pcg4d(v);  // the reference's own pcg4d (common/wltcRS.glsl)
   return vec4((float)(v.x >> 24) / 255.0f, (float)(v.y >> 24) / 255.0f, (float)(v.z >> 24) / 255.0f,
@@ -498,6 +506,11 @@ void ref_set_colors(void* h, const float ground[4], const float sky[4]) {
   c.ubo.sky_color = vec4(sky[0], sky[1], sky[2], sky[3]);
 }
 void ref_set_env_intensity(void* h, float v) { static_cast<Ctx*>(h)->ubo.env_intensity = v; }
+void ref_set_blue_noise(void* h, const unsigned char* rgba8) {
+  Ctx& c = *static_cast<Ctx*>(h);
+  if (rgba8) c.blue_noise.assign(rgba8, rgba8 + 4 * 1024 * 1024);
+  else c.blue_noise.clear();
+}
 void ref_set_exposure_value(void* h, float v) { static_cast<Ctx*>(h)->ubo.exposure_value = v; }
 
 int ref_commit(void* h) {

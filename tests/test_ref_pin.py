@@ -38,3 +38,21 @@ def test_golden_fixtures_are_current():
         g = np.load(os.path.join(HERE, "golden", f"ref_{name}.npz"))
         assert np.array_equal(r.image(0).view(np.uint32), g["accum"].view(np.uint32)), name
         assert np.array_equal(r.image(3), g["final"]), name
+
+
+@pytest.mark.parametrize("name", ["cornell", "thin_lens_reinhard", "ortho_sky"])
+def test_loaded_blue_noise_texture_matches_the_reference_shaders(oracle_mod, name):
+    """With a loaded blue-noise texture (load_blue_noise_texture) the
+    reference's rand4blue and camera shaders and the oracle give the same
+    images, bit for bit."""
+    sc = pin_scenes.PIN_SCENES[name]()
+    sc.blue_noise = np.random.default_rng(13).integers(0, 256, (1024, 1024, 4)).astype(np.uint8)
+    r = ref.RefRenderer(sc)
+    r.render(sc.spp)
+    o = oracle_mod.Oracle(sc)
+    o.render(sc.spp)
+    for which in (0, 1, 2, 3):
+        assert np.array_equal(r.image(which).view(np.uint32), o.image(which).view(np.uint32)), which
+    plain = oracle_mod.Oracle(pin_scenes.PIN_SCENES[name]())
+    plain.render(sc.spp)
+    assert not np.array_equal(plain.image(0), o.image(0))
