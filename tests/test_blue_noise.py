@@ -123,3 +123,43 @@ def test_loaded_texture_paths_match_the_oracle(pt, oracle_mod, tmp_path, name):
         a.load_blue_noise_texture(small)
     for x in (r, a, b, c):
         x.close()
+
+
+def test_mutated_pngs_are_read_or_refused(pt, tmp_path):
+    """Seeded byte mutations of PNGs of four layouts (chunk lengths, header
+    fields, compressed data): each is read or refused with a reason, never a
+    crash."""
+    import ctypes as C
+    import random
+    abi = importlib.import_module("hala-pathtracer_gb300.abi")
+    pt.build()
+    lib = pt.load_library()
+    rng = np.random.default_rng(1)
+    seeds = [_png(rng.integers(0, 256, (9, 7, 4)), 8, 6),
+             _png(rng.integers(0, 4, (5, 6, 1)), 2, 3, rng.integers(0, 256, 12).tolist(), [1, 2]),
+             _png(rng.integers(0, 65536, (3, 3, 3)), 16, 2), _png(rng.integers(0, 256, (4, 4, 2)), 8, 4)]
+    r = random.Random(3)
+    p = tmp_path / "m.png"
+    seen = {abi.PT_OK: 0, abi.PT_ERR_INVALID_ARG: 0}
+    for _ in range(600):
+        b = bytearray(r.choice(seeds))
+        for _ in range(r.randint(1, 4)):
+            k = r.randrange(len(b))
+            op = r.random()
+            if op < 0.5:
+                b[k] = r.randrange(256)
+            elif op < 0.7:
+                del b[k:k + r.randint(1, 8)]
+            elif op < 0.85:
+                b[k:k] = bytes(r.randrange(256) for _ in range(r.randint(1, 8)))
+            else:
+                b[k:k + 4] = r.choice([b"\xff\xff\xff\xff", b"\x7f\xff\xff\xff", b"\x00\x01\x00\x00", b"\0\0\0\0"])
+        p.write_bytes(bytes(b))
+        w, h = C.c_uint32(), C.c_uint32()
+        err = C.create_string_buffer(256)
+        st = lib.pt_png_read_rgba8(str(p).encode(), None, 0, C.byref(w), C.byref(h), err, 256)
+        assert st in seen, st
+        seen[st] += 1
+        if st != abi.PT_OK:
+            assert err.value
+    assert seen[abi.PT_OK] > 0 and seen[abi.PT_ERR_INVALID_ARG] > 0
