@@ -143,3 +143,48 @@ def test_files_the_reader_refuses(pt, gpu_lib, exr, tmp_path):
     refused(broken, "corrupt")
     with pytest.raises(pt.PTError, match="cannot open"):
         pt.read_exr(str(tmp_path / "missing.exr"))
+
+
+def test_mutated_files_are_read_or_refused(pt, exr, tmp_path):
+    """Seeded byte mutations of EXR files (header attributes, offset table,
+    chunk sizes, ZIP streams): each is read or refused with a reason, never a
+    crash."""
+    import ctypes as C
+    import random
+    abi = importlib.import_module("hala-pathtracer_gb300.abi")
+    pt.build()
+    lib = pt.load_library()
+    rng = np.random.default_rng(1)
+    seeds = []
+    for k, (half, comp) in enumerate([(False, "ZIP"), (True, "ZIP"), (False, "NONE"), (True, "NONE")]):
+        p = tmp_path / f"s{k}.exr"
+        exr.write(str(p), (rng.random((19, 23, 3)) * 5).astype(np.float32), half=half, compression=comp)
+        seeds.append(p.read_bytes())
+    r = random.Random(5)
+    p = tmp_path / "m.exr"
+    seen = {abi.PT_OK: 0, abi.PT_ERR_INVALID_ARG: 0}
+    for _ in range(600):
+        b = bytearray(r.choice(seeds))
+        for _ in range(r.randint(1, 4)):
+            k = r.randrange(len(b))
+            op = r.random()
+            if op < 0.5:
+                b[k] = r.randrange(256)
+            elif op < 0.7:
+                del b[k:k + r.randint(1, 8)]
+            elif op < 0.85:
+                b[k:k] = bytes(r.randrange(256) for _ in range(r.randint(1, 8)))
+            else:
+                b[k:k + 4] = r.choice([b"\xff\xff\xff\xff", b"\xff\xff\xff\x7f", b"\0\0\x01\0", b"\0\0\0\0"])
+        p.write_bytes(bytes(b))
+        w, h = C.c_uint32(), C.c_uint32()
+        err = C.create_string_buffer(256)
+        st = lib.pt_exr_read_rgb(str(p).encode(), None, 0, C.byref(w), C.byref(h), err, 256)
+        if st == abi.PT_OK:
+            out = np.empty((h.value, w.value, 3), np.float32)
+            st = lib.pt_exr_read_rgb(str(p).encode(), out.ctypes.data, out.size, C.byref(w), C.byref(h), err, 256)
+        assert st in seen, st
+        seen[st] += 1
+        if st != abi.PT_OK:
+            assert err.value
+    assert seen[abi.PT_OK] > 0 and seen[abi.PT_ERR_INVALID_ARG] > 0
