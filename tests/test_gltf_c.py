@@ -283,6 +283,20 @@ def test_malformed_files_are_refused_with_a_reason(pt, lib, tmp_path):
                                    "meshes": [{"primitives": [{"attributes": {"POSITION": 0}}]}],
                                    "accessors": [{"componentType": 5126, "count": 3, "type": "VEC3",
                                                   "sparse": {"count": 1}}]}),
+        "huge.gltf": json.dumps({"asset": {"version": "2.0"}, "scenes": [{"nodes": [0, 1]}],
+                                 "nodes": [{"mesh": 0}, {"camera": 0}], "cameras": [{"type": "perspective"}],
+                                 "meshes": [{"primitives": [{"attributes": {"POSITION": 0}}]}],
+                                 "accessors": [{"componentType": 5126, "count": 2147483647, "type": "MAT4"}]}),
+        "overrun.gltf": json.dumps({"asset": {"version": "2.0"}, "scenes": [{"nodes": [0, 1]}],
+                                    "nodes": [{"mesh": 0}, {"camera": 0}], "cameras": [{"type": "perspective"}],
+                                    "meshes": [{"primitives": [{"attributes": {"POSITION": 0}}]}],
+                                    "accessors": [{"bufferView": 0, "componentType": 5126, "count": 2147483647,
+                                                   "type": "VEC3", "byteOffset": 4}],
+                                    "bufferViews": [{"buffer": 0, "byteLength": 12, "byteStride": 4096}],
+                                    "buffers": [{"byteLength": 12, "uri": _uri(bytes(12))}]}),
+        "cycle.gltf": json.dumps({"asset": {"version": "2.0"}, "scenes": [{"nodes": [0]}],
+                                  "nodes": [{"children": [1], "camera": 0}, {"children": [0]}],
+                                  "cameras": [{"type": "perspective"}]}),
         "short.gltf": json.dumps({"asset": {"version": "2.0"}, "scenes": [{"nodes": [0, 1]}],
                                   "nodes": [{"mesh": 0}, {"camera": 0}], "cameras": [{"type": "perspective"}],
                                   "meshes": [{"primitives": [{"attributes": {"POSITION": 0}}]}],
